@@ -1,0 +1,371 @@
+"""Benchmark: DM-trial samples/s of the single-pulse search (unpack -> RFI -> subband
+dedispersion over the ddplan -> boxcar + threshold) on one GB300 per rank.
+
+A step is one pass of every ddplan row over a whole synthetic filterbank (all its blocks).
+`value` times the device work with the input already resident in HBM (txg_push_block_device);
+`e2e` times the public host-pointer call (txg_push_block from pinned host memory, H2D inside
+the timed region) plus the per-block candidate read-back and host clustering.  Ranks are
+independent beams (weak scaling, no collective on the data path).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+ELEM = {"fp32": 4, "bf16": 2, "fp16": 2}
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="nchan4096_n2M_rfi_dm3000")
+    ap.add_argument("--nsamples", type=int, default=0, help="override the file length")
+    ap.add_argument("--precision", choices=["fp32", "bf16", "fp16"], default="fp32")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-blocks", type=int, default=2, help="timed oracle blocks (CPU baseline)")
+    return ap.parse_args()
+
+
+# ---- clocks during the timed region -------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index, self.rows, self.proc = index, [], None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(self.rows)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ---- algorithmic bytes per kernel class (per launch, per row) ----------------------------
+def class_bytes(info, sp, nchans_raw, ndump_raw, ncand, elem):
+    """Bytes a perfect implementation must move for one launch of each class:
+    unpack: raw uint8 in + float block out; preprocess: read+write the block once;
+    stage 1: block in + subband series out; stage 2: subband series in + dedispersed out;
+    boxcar: dedispersed series in + 16-byte candidates out."""
+    C, N = info.nchans, info.ndump
+    block = 4.0 * C * N
+    series = float(elem) * info.nsub * info.ngroup * N
+    return [nchans_raw * ndump_raw + block, 2 * block, block + series,
+            series + 4.0 * info.ndm * info.nsamples, 4.0 * info.ndm * info.nsamples + 16 * ncand]
+
+
+def launches_per_block(sp, info, gated):
+    n = 2  # unpack, equalize
+    if info.nchans and sp.bswidth > 0:
+        n += 3
+    if sp.zaplist:
+        n += 1
+    for op in sp.rfilist:
+        n += 3 if op[0] == "kadaneF" else 4
+    n += 1  # stage 1
+    if gated:
+        n += 2  # stage 2, boxcar
+    return n
+
+
+# ---- reference arm / CPU baseline: the oracle port on the host cores ------------------------
+def cpu_reference(wl, steps, warmup, timed_blocks=None, nthreads=0):
+    """Oracle restatement of the path (oracle/txoracle.c) on the machine's host cores, row 0 of the
+    workload (its heaviest ddplan row): warm the row until it is gated, then time one block
+    per step.  Returns (value, seconds per step, sample description, cores)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    import transientx_gb300 as tx
+    O.build(ref=False)
+    cores = nthreads or os.cpu_count()
+    O.lib().txo_set_threads(cores)
+    sp = wl.rows[0]
+    info = tx.describe_row(wl.rows, 0, wl.fil.nchans, wl.fil.tsamp, wl.fil.freqs, wl.ndump)[0]
+    row = O.make_row(td=sp.td, fd=sp.fd, bswidth=sp.bswidth, rfi=sp.rfilist,
+                     threKadaneF=sp.threKadaneF, widthlimit=sp.widthlimit, dms=sp.dms,
+                     ddm=sp.ddm, ndm=sp.ndm, overlap=sp.overlap, nsub=info.nsub,
+                     group=info.dm_group, minw=sp.minw, maxw=sp.maxw, snrloss=sp.snrloss,
+                     thre=sp.thre)
+    orow = O.SinglePulseRow(row, wl.fil.freqs, wl.fil.tsamp, wl.ndump)
+    b = 0
+    while True:  # fill the DM-delay history (not timed)
+        raw = wl.fil.generate(b * wl.ndump, wl.ndump)
+        b += 1
+        if orow.run(raw):
+            break
+    n = (timed_blocks if timed_blocks else steps + warmup)
+    times = []
+    for k in range(n):
+        raw = wl.fil.generate(b * wl.ndump, wl.ndump)
+        b += 1
+        t = time.perf_counter()
+        assert orow.run(raw)
+        times.append(time.perf_counter() - t)
+    timed = times[warmup:] if not timed_blocks else times
+    per = float(np.mean(timed))
+    work = info.ndm * info.nsamples
+    sample = (f"row 0 of {wl.name} (td={sp.td}, {sp.ndm} DMs, {info.nchans} channels, "
+              f"{info.ndump}-sample blocks): {len(timed)} gated blocks timed after "
+              f"{b - len(times)} history blocks")
+    return work / per, per, sample, cores
+
+
+def run_reference(args, wl):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    value, per, sample, cores = cpu_reference(wl, args.steps, args.warmup)
+    line = {"metric": "DM-trial samples/s", "value": value, "unit": "DM-trial samples/s",
+            "impl": "reference", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": wl.name, "sample": "one gated block of ddplan row 0 per step"},
+            "cpu_baseline": {"value": value, "unit": "DM-trial samples/s", "cores": cores,
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "DM-trial samples/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---- our arm ------------------------------------------------------------------------------
+def run_ours(args, wl):
+    import torch
+    import transientx_gb300 as tx
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    fil = wl.fil
+    if world > 1:  # each rank searches its own beam
+        fil.seed = fil.seed + rank
+    nblk = fil.nsamples // wl.ndump
+    host = torch.empty((nblk * wl.ndump, fil.nchans), dtype=torch.uint8, pin_memory=True)
+    fil.generate(0, nblk * wl.ndump, out=host.numpy())
+    dev = host.to("cuda", non_blocking=False)
+    base = dev.data_ptr()
+    blk_bytes = wl.ndump * fil.nchans
+
+    flags = tx.FLAG_TIMING
+    s = tx.Search(wl.rows, fil.nchans, fil.tsamp, fil.freqs, wl.ndump, precision=args.precision,
+                  flags=flags)
+    infos = [s.row_info(r) for r in range(len(wl.rows))]
+    stream = torch.cuda.ExternalStream(s.stream())
+
+    def drain(stats):
+        for r in range(len(wl.rows)):
+            while True:
+                res = s.pop_result(r)
+                if res is None:
+                    break
+                _, gated, cands, n = res
+                if gated:
+                    stats["work"] += infos[r].ndm * infos[r].nsamples
+                    stats["ncand"][r] += n
+                    stats["gated"][r] += 1
+                    stats["launches"] += launches_per_block(wl.rows[r], infos[r], True)
+                else:
+                    stats["launches"] += launches_per_block(wl.rows[r], infos[r], False)
+
+    def new_stats():
+        return {"work": 0, "ncand": [0] * len(wl.rows), "gated": [0] * len(wl.rows),
+                "launches": 0, "d2h": 0}
+
+    def step_device(stats):
+        for b in range(nblk):
+            s.push_block_device(base + b * blk_bytes)
+            drain(stats)
+        s.sync(allow_overflow=True)
+        drain(stats)
+
+    for _ in range(args.warmup):
+        step_device(new_stats())
+    s.timing()  # reset the per-class accumulators
+    stats = new_stats()
+    clocks = ClockSampler(local)
+    barrier()
+    clocks.start()
+    t_host = time.perf_counter()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step_device(stats)
+    e1.record(stream)
+    barrier()
+    t_host = time.perf_counter() - t_host
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    cls_ms, cls_n = s.timing()
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    work_total = stats["work"] * world
+    value = work_total / (ms / 1e3)
+
+    # dominant kernel class and its roofline
+    names = ["unpack", "preprocess", "stage1", "stage2", "boxcar"]
+    top = int(np.argmax(cls_ms))
+    nb_total = [0.0] * 5
+    for r, (sp, info) in enumerate(zip(wl.rows, infos)):
+        nblocks_r = stats["gated"][r]  # every timed block is gated after the warm-up
+        ncand_avg = stats["ncand"][r] / max(1, stats["gated"][r])
+        cb = class_bytes(info, sp, fil.nchans, wl.ndump, ncand_avg, ELEM[args.precision])
+        for c in range(5):
+            nb_total[c] += cb[c] * (args.steps * nblk if c < 3 else nblocks_r)
+    peak, peak_kind = measured_peaks()
+    achieved = nb_total[top] / (cls_ms[top] / 1e3) / 1e9
+    roof = {"bound": "hbm", "kernel": names[top], "achieved": achieved, "peak": peak,
+            "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+            "peak_source": peak_kind,
+            "class_ms": {names[c]: float(cls_ms[c]) for c in range(5)},
+            "class_launches": {names[c]: int(cls_n[c]) for c in range(5)},
+            "class_algorithmic_GBps": {names[c]: (nb_total[c] / (cls_ms[c] / 1e3) / 1e9
+                                                   if cls_ms[c] > 0 else None) for c in range(5)}}
+
+    e2e = None
+    if not args.no_e2e:
+        hpin = host.numpy()
+
+        def step_host(st):
+            for b in range(nblk):
+                s.push_block(hpin[b * wl.ndump:(b + 1) * wl.ndump])
+                for r in range(len(wl.rows)):
+                    while True:
+                        res = s.pop_result(r)
+                        if res is None:
+                            break
+                        _, gated, cands, n = res
+                        st["d2h"] += 8 + 16 * len(cands)
+                        if gated:
+                            st["work"] += infos[r].ndm * infos[r].nsamples
+                            s.cluster(r, cands=cands)
+            s.sync(allow_overflow=True)
+            for r in range(len(wl.rows)):
+                while True:
+                    res = s.pop_result(r)
+                    if res is None:
+                        break
+                    _, gated, cands, n = res
+                    st["d2h"] += 8 + 16 * len(cands)
+                    if gated:
+                        st["work"] += infos[r].ndm * infos[r].nsamples
+                        s.cluster(r, cands=cands)
+
+        step_host(new_stats())
+        st = new_stats()
+        barrier()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            step_host(st)
+        f1.record(stream)
+        barrier()
+        wall = time.perf_counter() - t0
+        e2e = {"value": st["work"] * world / wall, "unit": "DM-trial samples/s",
+               "h2d_bytes_per_step": nblk * blk_bytes,
+               "d2h_bytes_per_step": st["d2h"] // max(1, args.steps),
+               "includes": "H2D from pinned host memory, candidate read-back, host clustering"}
+    s.close()
+
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu:
+        v, per, sample, cores = cpu_reference(wl, 0, 0, timed_blocks=args.cpu_blocks)
+        cpu = {"value": v, "unit": "DM-trial samples/s", "cores": cores, "kind": "port",
+               "sample": sample}
+    line = {"metric": "DM-trial samples/s", "value": value, "unit": "DM-trial samples/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else
+            f"{args.precision} storage, f32 accumulate", "data": "synthetic",
+            "config": {"workload": wl.name, "nchans": fil.nchans, "tsamp": fil.tsamp,
+                       "nsamples": nblk * wl.ndump, "ndump": wl.ndump, "nblocks": nblk,
+                       "rows": [[sp.td, sp.dms, sp.ddm, sp.ndm] for sp in wl.rows],
+                       "nsub": [i.nsub for i in infos], "dm_group": [i.dm_group for i in infos],
+                       "precision": args.precision, "parallelism": f"beam-per-gpu x{world}",
+                       "l2": "inputs larger than L2 (raw file %.1f GB)" % (host.numel() / 1e9)},
+            "clocks": clk, "e2e": e2e, "gpu_launches": stats["launches"],
+            "roofline": roof, "cpu_baseline": cpu,
+            "work_per_step": stats["work"] / args.steps, "host_wall_s": t_host}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    from transientx_gb300 import synth
+    make = synth.WORKLOADS[args.workload]
+    wl = make(nsamples=args.nsamples) if args.nsamples else make()
+    if args.impl == "reference":
+        run_reference(args, wl)
+    else:
+        run_ours(args, wl)
+
+
+if __name__ == "__main__":
+    main()

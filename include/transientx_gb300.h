@@ -1,0 +1,196 @@
+/*
+ * transientx_gb300.h -- C ABI of the GB300 (sm_103a) implementation of TransientX's per-block
+ * single-pulse search: unpack -> downsample -> equalize -> baseline -> RFI (zap, kadaneF,
+ * zdot) -> two-stage subband dedispersion -> boxcar matched filter -> S/N threshold.
+ *
+ * Plain C types only; every function returns a txg_status (0 = success, < 0 = error) unless
+ * noted.  One handle owns its device memory and CUDA stream; calls on one handle must be
+ * serialised by the caller, different handles are independent.  No exceptions cross this
+ * boundary.  Paths below are relative to the TransientX source tree.
+ */
+#ifndef TRANSIENTX_GB300_H
+#define TRANSIENTX_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TXG_ABI_VERSION 1
+
+typedef enum {
+    TXG_OK = 0,
+    TXG_ERR_ARG = -1,          /* invalid argument or plan */
+    TXG_ERR_NOMEM = -2,        /* device or pinned-host allocation failed */
+    TXG_ERR_CUDA = -3,         /* CUDA runtime error (context still usable) */
+    TXG_ERR_OVERFLOW = -4,     /* candidate buffer overflowed; raise cand_capacity */
+    TXG_ERR_TIMEOUT = -5,      /* a bounded device wait gave up */
+    TXG_ERR_STATE = -6,        /* call not valid in the handle's current state */
+    TXG_ERR_NODEVICE = -7,     /* no CUDA device / extension unusable */
+    TXG_ERR_UNSUPPORTED = -8   /* option not implemented for these sizes */
+} txg_status;
+
+typedef enum { TXG_RFI_KADANEF = 1, TXG_RFI_ZDOT = 2 } txg_rfi_kind;
+
+typedef enum {
+    TXG_PREC_FP32 = 0,         /* subband series and prefix sums in FP32 (reference arithmetic) */
+    TXG_PREC_BF16 = 1,         /* subband series stored as BF16, FP32 accumulation */
+    TXG_PREC_FP16 = 2          /* subband series stored as FP16, FP32 accumulation */
+} txg_precision;
+
+typedef enum {
+    TXG_FLAG_AVX2_TAIL = 1,    /* reproduce the -mavx2 build's per-width range of boxcar.cpp:264-279 */
+    TXG_FLAG_DENSE = 2,        /* keep dense mxS/mxwn (Boxcar::mxS/mxwn, include/boxcar.h:40-41) */
+    TXG_FLAG_KEEP_SERIES = 4,  /* keep preprocessed block and dedispersed series for inspection */
+    TXG_FLAG_TIMING = 8        /* bracket each kernel class with CUDA events (txg_get_timing) */
+} txg_flags;
+
+/* One ddplan row: the fields of SinglePulse that SinglePulse::prepare/run read
+ * (include/singlepulse.h:95-133, src/singlepulse/singlepulse.cpp:206-341). */
+typedef struct {
+    int32_t td, fd;            /* Downsample (singlepulse.cpp:208-209) */
+    float bswidth;             /* BaseLine width in s, <= 0 disables (singlepulse.cpp:218) */
+    int32_t nrfi;              /* rfilist entries, run in order (singlepulse.cpp:298-325) */
+    int32_t rfi_kind[8];       /* txg_rfi_kind */
+    int32_t rfi_td[8], rfi_fd[8];
+    int32_t nzap;              /* zaplist (singlepulse.cpp:295) */
+    double zap[16][2];         /* [fl, fh] in MHz */
+    float threKadaneF;         /* S/N threshold of kadaneF (squared before use, :307) */
+    double widthlimit;         /* kadaneF minimum window in s (:307) */
+    double dms, ddm;           /* SubbandDedispersion dms/ddm/ndm/overlap (:230-233) */
+    int64_t ndm;
+    double overlap;
+    float minw, maxw, snrloss; /* boxcar width ladder (singlepulse.cpp:242-254) */
+    int32_t iqr;               /* Boxcar::run iqr argument (boxcar.cpp:204-227) */
+    float thre;                /* S/N threshold (cluster.cpp:95) */
+    int32_t nsub;              /* subbands; 0 = automatic */
+    int32_t dm_group;          /* fine DMs per coarse DM; 0 = automatic */
+} txg_row;
+
+typedef struct {
+    int32_t nchans;            /* raw channels */
+    double tsamp;              /* raw sampling time (s) */
+    const double *frequencies; /* nchans channel centre frequencies (MHz) */
+    int64_t ndump;             /* raw samples per block (dedisperse_fil.cpp:244) */
+    int32_t nrows;
+    const txg_row *rows;
+    int32_t nbeams;            /* independent beams sharing the plan */
+    int32_t precision;         /* txg_precision */
+    int32_t flags;             /* txg_flags */
+    int64_t cand_capacity;     /* candidates kept per (beam,row,block); 0 = default */
+} txg_plan;
+
+/* One point above threshold, in the order Cluster::run scans mxS (cluster.cpp:91-112). */
+typedef struct {
+    int32_t idm;
+    int32_t isamp;
+    int32_t wn;
+    float S;
+} txg_cand;
+
+/* Geometry of one row: the public members of SubbandDedispersion and Boxcar that the
+ * reference reads (boxcar.cpp:142-161, cluster.cpp:65-117, candplot.cpp:47). */
+typedef struct {
+    int32_t nchans, nsub, dm_group, ngroup, nwidths, maxwn;
+    int64_t ndm, ndump, noverlap, offset, nsamples, counter, maxd1, maxd2;
+    double tsamp, dms, ddm, fmin, fmax;
+    int32_t gated;             /* 1 if the last block produced boxcar output */
+    int32_t pad;
+} txg_row_info;
+
+typedef struct txg_handle txg_handle;
+
+/* Plan all ddplan rows and allocate device state: SinglePulse::prepare for every row
+ * (singlepulse.cpp:206-254) plus Boxcar::prepare (boxcar.cpp:142-156). */
+int txg_create(const txg_plan *plan, txg_handle **out);
+void txg_destroy(txg_handle *h);
+
+/* Feed one block of raw uint8 time-major samples [nsamp][nchans] for one beam and run every
+ * ddplan row on it: the body of the transientx_fil block loop (dedisperse_fil.cpp:324-337)
+ * calling SinglePulse::run (singlepulse.cpp:287-341).  nsamp must equal the plan's ndump.
+ * The host variant copies through pinned staging buffers; the call returns once the block
+ * is queued and the caller's buffer may be reused. */
+int txg_push_block(txg_handle *h, int32_t beam, const uint8_t *host, int64_t nsamp);
+int txg_push_block_device(txg_handle *h, int32_t beam, const uint8_t *dev, int64_t nsamp);
+
+/* Wait for queued work and collect candidates; returns TXG_ERR_OVERFLOW if any buffer
+ * overflowed since the last call. */
+int txg_sync(txg_handle *h);
+
+int txg_get_row_info(txg_handle *h, int32_t beam, int32_t row, txg_row_info *out);
+
+/* Points with S > thre of the last block of (beam,row), sorted by (idm, isamp): the input
+ * Cluster::run builds from mxS (cluster.cpp:84-112).  *n receives the full count. */
+int txg_get_candidates(txg_handle *h, int32_t beam, int32_t row, txg_cand *out, int64_t cap,
+                       int64_t *n);
+
+/* Per-block results in push order: pops the oldest harvested block of (beam,row) not yet
+ * popped (up to 256 are kept; older ones are dropped).  *counter is the row's sample counter
+ * after that block (Boxcar::counter, boxcar.cpp:160), *gated whether it produced boxcar
+ * output, *n the number of S > thre points (written to out up to cap, sorted as in
+ * txg_get_candidates).  Returns TXG_ERR_STATE when no block is waiting. */
+int txg_pop_result(txg_handle *h, int32_t beam, int32_t row, int64_t *counter, int32_t *gated,
+                   txg_cand *out, int64_t cap, int64_t *n);
+
+/* Dense Boxcar::mxS / mxwn of the last block (plan flag TXG_FLAG_DENSE): [ndm][nsamples]. */
+int txg_get_dense(txg_handle *h, int32_t beam, int32_t row, float *mxS, int32_t *mxwn);
+
+/* SubbandDedispersion::get_timdata(tim, idm, true) for idm0..idm0+count-1 of the last block
+ * (boxcar.cpp:183; plan flag TXG_FLAG_KEEP_SERIES): [count][nsamples]. */
+int txg_get_timdata(txg_handle *h, int32_t beam, int32_t row, int64_t idm0, int64_t count,
+                    float *out);
+
+/* The row's preprocessed block after the rfilist ([nchans][ndump], TXG_FLAG_KEEP_SERIES),
+ * and the kadaneF windows of rfilist entry irfi ([nchans/fd][4]: start,end of the positive
+ * and negative window in block samples, -1 if not zapped). */
+int txg_get_block(txg_handle *h, int32_t beam, int32_t row, float *out);
+int txg_get_zap_ranges(txg_handle *h, int32_t beam, int32_t row, int32_t irfi, int32_t *out,
+                       int64_t cap);
+
+/* Integer tables of a row: within-subband delays d1 [ngroup][nchans], subband delays
+ * d2 [ndm][nsub], first channel of each subband [nsub+1], width ladder [nwidths]. */
+int txg_get_tables(txg_handle *h, int32_t row, int32_t *d1, int32_t *d2, int32_t *sub_start,
+                   int32_t *vwn);
+
+/* Plan one row without a device (host only): fills info (counter 0) and, when non-NULL, the
+ * tables of txg_get_tables.  Lets a caller size buffers before txg_create. */
+int txg_describe_row(const txg_plan *plan, int32_t row, txg_row_info *info, int32_t *d1,
+                     int32_t *d2, int32_t *sub_start, int32_t *vwn);
+
+/* Boxcar width ladder of SinglePulse::prepare (singlepulse.cpp:242-254); returns the count. */
+int txg_width_ladder(float minw, float maxw, float snrloss, double tsamp, int32_t *vwn,
+                     int32_t cap);
+
+/* Boxcar::run over series supplied by the caller (boxcar.cpp:158-296): tim [ndm][nsamples]
+ * host memory; writes dense mxS/mxwn when non-NULL and the S > thre points (sorted) when
+ * cands is non-NULL.  flags: TXG_FLAG_AVX2_TAIL. */
+int txg_boxcar(const float *tim, int64_t ndm, int64_t nsamples, const int32_t *vwn, int32_t nw,
+               int32_t iqr, int32_t flags, float thre, float *mxS, int32_t *mxwn,
+               txg_cand *cands, int64_t cap, int64_t *ncand);
+
+/* Cluster<double>::run (cluster.cpp:63-161, clustering.h:26-100) on a sorted candidate list;
+ * out receives the reported candidates (idm, isamp, wn, S) in the reference's order. */
+int txg_cluster(const txg_cand *cands, int64_t n, double dms, double ddm, double fmax,
+                double fmin, double tsamp, double radius_smearing, int32_t maxncand,
+                int32_t minpts, int32_t drop, int32_t maxwn, txg_cand *out, int64_t cap,
+                int64_t *nout);
+
+/* Device time per kernel class accumulated since the last call (plan flag TXG_FLAG_TIMING),
+ * measured with CUDA events on the handle's stream: ms[c] total milliseconds and launches[c]
+ * number of launches of class c; classes 0 unpack, 1 preprocess+RFI, 2 stage 1,
+ * 3 stage 2, 4 boxcar.  Returns the number of classes. */
+int txg_get_timing(txg_handle *h, double *ms, int64_t *launches, int32_t n);
+
+/* The handle's CUDA stream (cudaStream_t) so callers can order or time work against it. */
+int txg_get_stream(txg_handle *h, void **stream);
+
+const char *txg_strerror(int32_t status);
+int32_t txg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TRANSIENTX_GB300_H */

@@ -1,0 +1,416 @@
+"""ctypes bindings for the CPU oracle (libtxoracle.so) and for the reference's own
+Boxcar/Cluster compiled in place (oracle/_ref/libtxref_*.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()`` and by the
+CPU-baseline leg of bench.py, never by the product package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_TREE = "/root/reference"
+
+f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+i64p = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
+u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+
+RFI_KADANEF = 1
+RFI_ZDOT = 2
+
+
+def build(ref: bool = True) -> None:
+    """Compile the oracle; also the reference harness when the reference tree is present."""
+    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    if ref and os.path.isdir(REF_TREE):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_TREE}"], check=True)
+
+
+class Cand(C.Structure):
+    _fields_ = [("idm", C.c_int64), ("isamp", C.c_int64), ("wn", C.c_int32), ("S", C.c_float)]
+
+
+CAND_DTYPE = np.dtype([("idm", "<i8"), ("isamp", "<i8"), ("wn", "<i4"), ("S", "<f4")])
+assert CAND_DTYPE.itemsize == C.sizeof(Cand)
+
+
+class DedispInfo(C.Structure):
+    _fields_ = [
+        ("nchan", C.c_int), ("nsub", C.c_int), ("group", C.c_int), ("ngroup", C.c_int),
+        ("ndm", C.c_long), ("ndump", C.c_long), ("maxd1", C.c_long), ("maxd2", C.c_long),
+        ("noverlap", C.c_long), ("offset", C.c_long), ("ring", C.c_long), ("nout", C.c_long),
+        ("counter", C.c_long), ("tsamp", C.c_double), ("fmax", C.c_double),
+        ("fmin", C.c_double),
+    ]
+
+
+class Row(C.Structure):
+    _fields_ = [
+        ("td", C.c_int), ("fd", C.c_int), ("bswidth", C.c_float), ("nrfi", C.c_int),
+        ("rfi_kind", C.c_int * 8), ("rfi_td", C.c_int * 8), ("rfi_fd", C.c_int * 8),
+        ("nzap", C.c_int), ("zap", (C.c_double * 2) * 16), ("threKadaneF", C.c_float),
+        ("widthlimit", C.c_double), ("dms", C.c_double), ("ddm", C.c_double),
+        ("ndm", C.c_long), ("overlap", C.c_double), ("nsub", C.c_int), ("group", C.c_int),
+        ("minw", C.c_float), ("maxw", C.c_float), ("snrloss", C.c_float), ("iqr", C.c_int),
+        ("avx2_tail", C.c_int), ("thre", C.c_float),
+    ]
+
+
+def make_row(**kw) -> Row:
+    r = Row()
+    r.td, r.fd = kw.get("td", 1), kw.get("fd", 1)
+    r.bswidth = kw.get("bswidth", 0.0)
+    rfi = kw.get("rfi", [])
+    r.nrfi = len(rfi)
+    for i, op in enumerate(rfi):
+        if op[0] == "kadaneF":
+            r.rfi_kind[i], r.rfi_td[i], r.rfi_fd[i] = RFI_KADANEF, int(op[1]), int(op[2])
+        elif op[0] == "zdot":
+            r.rfi_kind[i], r.rfi_td[i], r.rfi_fd[i] = RFI_ZDOT, 1, 1
+        else:
+            raise ValueError(f"unsupported rfi op {op}")
+    zap = kw.get("zap", [])
+    r.nzap = len(zap)
+    for i, (a, b) in enumerate(zap):
+        r.zap[i][0], r.zap[i][1] = a, b
+    r.threKadaneF = kw.get("threKadaneF", 7.0)
+    r.widthlimit = kw.get("widthlimit", 50e-3)
+    r.dms, r.ddm, r.ndm = kw["dms"], kw["ddm"], kw["ndm"]
+    r.overlap = kw.get("overlap", 0.0)
+    r.nsub, r.group = kw["nsub"], kw["group"]
+    r.minw, r.maxw, r.snrloss = kw.get("minw", 1e-4), kw["maxw"], kw.get("snrloss", 0.1)
+    r.iqr = int(kw.get("iqr", False))
+    r.avx2_tail = int(kw.get("avx2_tail", False))
+    r.thre = kw.get("thre", 7.0)
+    return r
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = os.path.join(HERE, "libtxoracle.so")
+    if not os.path.exists(path):
+        build(ref=False)
+    L = C.CDLL(path)
+    L.txo_dmdelay.restype = C.c_double
+    L.txo_dmdelay.argtypes = [C.c_double] * 3
+    L.txo_width_ladder.restype = C.c_int
+    L.txo_width_ladder.argtypes = [C.c_float, C.c_float, C.c_float, C.c_double, i32p, C.c_int]
+    L.txo_kadane.restype = C.c_float
+    L.txo_kadane.argtypes = [f32p, C.c_long, C.POINTER(C.c_long), C.POINTER(C.c_long)]
+    L.txo_red32.restype = C.c_double
+    L.txo_red32.argtypes = [f32p, C.c_void_p, C.c_long, C.c_int]
+    L.txo_unpack_downsample.argtypes = [u8p, C.c_long, C.c_int, C.c_int, C.c_int, f32p, C.c_long]
+    L.txo_downsample_freqs.argtypes = [f64p, C.c_int, C.c_int, f64p]
+    L.txo_equalize.argtypes = [f32p, C.c_int, C.c_long, C.c_long]
+    L.txo_baseline.argtypes = [f32p, C.c_int, C.c_long, C.c_long, C.c_long]
+    L.txo_zap_channels.argtypes = [f32p, C.c_int, C.c_long, C.c_long, f64p, f64p, C.c_int]
+    L.txo_kadaneF.restype = C.c_int
+    L.txo_kadaneF.argtypes = [f32p, C.c_int, C.c_long, C.c_long, C.c_int, C.c_int, C.c_float,
+                              C.c_long, i32p]
+    L.txo_zdot.argtypes = [f32p, C.c_int, C.c_long, C.c_long]
+    L.txo_boxcar_match.argtypes = [f32p, C.c_long, i32p, C.c_int, C.c_int, C.c_int, f32p, i32p]
+    L.txo_boxcar_run.argtypes = [f32p, C.c_long, C.c_long, i32p, C.c_int, C.c_int, C.c_int,
+                                 f32p, i32p]
+    L.txo_threshold_scan.restype = C.c_long
+    L.txo_threshold_scan.argtypes = [f32p, i32p, C.c_long, C.c_long, C.c_float, C.c_void_p,
+                                     C.c_long]
+    L.txo_cluster.restype = C.c_long
+    L.txo_cluster.argtypes = [C.c_void_p, C.c_long, C.c_double, C.c_double, C.c_double,
+                              C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int,
+                              C.c_int, C.c_void_p, C.c_void_p]
+    L.txo_dedisp_create.restype = C.c_void_p
+    L.txo_dedisp_create.argtypes = [C.c_int, f64p, C.c_double, C.c_long, C.c_double,
+                                    C.c_double, C.c_long, C.c_double, C.c_int, C.c_int]
+    L.txo_dedisp_destroy.argtypes = [C.c_void_p]
+    L.txo_dedisp_get_info.argtypes = [C.c_void_p, C.POINTER(DedispInfo)]
+    L.txo_dedisp_tables.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.txo_dedisp_run.restype = C.c_int
+    L.txo_dedisp_run.argtypes = [C.c_void_p, f32p, C.c_long]
+    L.txo_dedisp_timdata.restype = C.POINTER(C.c_float)
+    L.txo_dedisp_timdata.argtypes = [C.c_void_p]
+    L.txo_sp_create.restype = C.c_void_p
+    L.txo_sp_create.argtypes = [C.POINTER(Row), C.c_int, f64p, C.c_double, C.c_long]
+    L.txo_sp_destroy.argtypes = [C.c_void_p]
+    L.txo_sp_run.restype = C.c_int
+    L.txo_sp_run.argtypes = [C.c_void_p, u8p]
+    L.txo_sp_nwidths.restype = C.c_int
+    L.txo_sp_nwidths.argtypes = [C.c_void_p, i32p, C.c_int]
+    L.txo_sp_dedisp_info.argtypes = [C.c_void_p, C.POINTER(DedispInfo)]
+    L.txo_sp_block.restype = C.POINTER(C.c_float)
+    L.txo_sp_block.argtypes = [C.c_void_p, C.POINTER(C.c_long), C.POINTER(C.c_int),
+                               C.POINTER(C.c_long)]
+    L.txo_sp_zap_ranges.restype = C.POINTER(C.c_int32)
+    L.txo_sp_zap_ranges.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int)]
+    L.txo_sp_timdata.restype = C.POINTER(C.c_float)
+    L.txo_sp_timdata.argtypes = [C.c_void_p]
+    L.txo_sp_mxS.restype = C.POINTER(C.c_float)
+    L.txo_sp_mxS.argtypes = [C.c_void_p]
+    L.txo_sp_mxwn.restype = C.POINTER(C.c_int)
+    L.txo_sp_mxwn.argtypes = [C.c_void_p]
+    L.txo_sp_freqs.argtypes = [C.c_void_p, f64p]
+    L.txo_set_threads.argtypes = [C.c_int]
+    _lib = L
+    return L
+
+
+# ---- thin numpy wrappers -------------------------------------------------------------------
+
+def dmdelay(dm, fh, fl):
+    return lib().txo_dmdelay(dm, fh, fl)
+
+
+def width_ladder(minw, maxw, snrloss, tsamp, cap=256):
+    out = np.zeros(cap, np.int32)
+    n = lib().txo_width_ladder(minw, maxw, snrloss, tsamp, out, cap)
+    return out[:n].copy()
+
+
+def kadane(y):
+    y = np.ascontiguousarray(y, np.float32)
+    s, e = C.c_long(), C.c_long()
+    b = lib().txo_kadane(y, len(y), C.byref(s), C.byref(e))
+    return float(np.float32(b)), s.value, e.value
+
+
+def red32(x, y=None, mode=0):
+    x = np.ascontiguousarray(x, np.float32)
+    yp = None
+    if y is not None:
+        y = np.ascontiguousarray(y, np.float32)
+        yp = y.ctypes.data
+    return lib().txo_red32(x, yp, len(x), mode)
+
+
+def unpack_downsample(raw, td=1, fd=1):
+    raw = np.ascontiguousarray(raw, np.uint8)
+    n0, nchan = raw.shape
+    x = np.zeros((nchan // fd, n0 // td), np.float32)
+    lib().txo_unpack_downsample(raw, n0, nchan, td, fd, x, x.shape[1])
+    return x
+
+
+def downsample_freqs(f, fd):
+    f = np.ascontiguousarray(f, np.float64)
+    out = np.zeros(len(f) // fd, np.float64)
+    lib().txo_downsample_freqs(f, len(f), fd, out)
+    return out
+
+
+def equalize(x):
+    x = np.array(x, np.float32, order="C", copy=True)
+    lib().txo_equalize(x, x.shape[0], x.shape[1], x.shape[1])
+    return x
+
+
+def baseline(x, nw):
+    x = np.array(x, np.float32, order="C", copy=True)
+    lib().txo_baseline(x, x.shape[0], x.shape[1], x.shape[1], nw)
+    return x
+
+
+def kadaneF(x, tdk, fdk, thr, wnlimit):
+    x = np.array(x, np.float32, order="C", copy=True)
+    ranges = np.zeros((x.shape[0] // fdk, 4), np.int32)
+    lib().txo_kadaneF(x, x.shape[0], x.shape[1], x.shape[1], tdk, fdk, thr, wnlimit, ranges)
+    return x, ranges
+
+
+def zdot(x):
+    x = np.array(x, np.float32, order="C", copy=True)
+    lib().txo_zdot(x, x.shape[0], x.shape[1], x.shape[1])
+    return x
+
+
+def boxcar_run(tim, vwn, iqr=False, avx2_tail=False):
+    tim = np.ascontiguousarray(tim, np.float32)
+    ndm, n = tim.shape
+    vwn = np.ascontiguousarray(vwn, np.int32)
+    mxS = np.zeros((ndm, n), np.float32)
+    mxwn = np.zeros((ndm, n), np.int32)
+    lib().txo_boxcar_run(tim, ndm, n, vwn, len(vwn), int(iqr), int(avx2_tail), mxS, mxwn)
+    return mxS, mxwn
+
+
+def threshold_scan(mxS, mxwn, thre):
+    mxS = np.ascontiguousarray(mxS, np.float32)
+    mxwn = np.ascontiguousarray(mxwn, np.int32)
+    cnt = lib().txo_threshold_scan(mxS, mxwn, mxS.shape[0], mxS.shape[1], thre, None, 0)
+    out = np.zeros(cnt, CAND_DTYPE)
+    lib().txo_threshold_scan(mxS, mxwn, mxS.shape[0], mxS.shape[1], thre, out.ctypes.data, cnt)
+    return out
+
+
+def cluster(cands, dms, ddm, fmax, fmin, tsamp, radius, maxncand, minpts, drop, maxwn):
+    cands = np.ascontiguousarray(cands, CAND_DTYPE)
+    out = np.zeros(max(len(cands), 1), CAND_DTYPE)
+    sizes = np.zeros(max(len(cands), 1), np.int32)
+    n = lib().txo_cluster(cands.ctypes.data, len(cands), dms, ddm, fmax, fmin, tsamp, radius,
+                          maxncand, minpts, int(drop), maxwn, out.ctypes.data, sizes.ctypes.data)
+    return out[:n].copy(), sizes[:n].copy()
+
+
+class Dedisp:
+    """Streaming two-stage subband dedispersion (oracle)."""
+
+    def __init__(self, freqs, tsamp, ndump, dms, ddm, ndm, overlap, nsub, group):
+        f = np.ascontiguousarray(freqs, np.float64)
+        self.h = lib().txo_dedisp_create(len(f), f, tsamp, ndump, dms, ddm, ndm, overlap, nsub,
+                                         group)
+        if not self.h:
+            raise ValueError("invalid dedispersion parameters")
+        self.nchan = len(f)
+        self.ndm = ndm
+
+    def info(self) -> DedispInfo:
+        i = DedispInfo()
+        lib().txo_dedisp_get_info(self.h, C.byref(i))
+        return i
+
+    def tables(self):
+        i = self.info()
+        d1 = np.zeros((i.ngroup, i.nchan), np.int32)
+        d2 = np.zeros((i.ndm, i.nsub), np.int32)
+        ss = np.zeros(i.nsub + 1, np.int32)
+        fr = np.zeros(i.nsub, np.float64)
+        lib().txo_dedisp_tables(self.h, d1.ctypes.data, d2.ctypes.data, ss.ctypes.data,
+                                fr.ctypes.data)
+        return d1, d2, ss, fr
+
+    def run(self, x):
+        x = np.ascontiguousarray(x, np.float32)
+        return bool(lib().txo_dedisp_run(self.h, x, x.shape[1]))
+
+    def timdata(self):
+        i = self.info()
+        p = lib().txo_dedisp_timdata(self.h)
+        return np.ctypeslib.as_array(p, shape=(i.ndm, i.nout)).copy()
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().txo_dedisp_destroy(self.h)
+            self.h = None
+
+
+class SinglePulseRow:
+    """One ddplan row of the SinglePulse::run chain (oracle)."""
+
+    def __init__(self, row: Row, freqs, tsamp, ndump):
+        f = np.ascontiguousarray(freqs, np.float64)
+        self.row = row
+        self.h = lib().txo_sp_create(C.byref(row), len(f), f, tsamp, ndump)
+        if not self.h:
+            raise ValueError("invalid row parameters")
+
+    def run(self, raw) -> bool:
+        raw = np.ascontiguousarray(raw, np.uint8)
+        return bool(lib().txo_sp_run(self.h, raw))
+
+    def info(self) -> DedispInfo:
+        i = DedispInfo()
+        lib().txo_sp_dedisp_info(self.h, C.byref(i))
+        return i
+
+    def widths(self):
+        out = np.zeros(256, np.int32)
+        n = lib().txo_sp_nwidths(self.h, out, 256)
+        return out[:n].copy()
+
+    def block(self):
+        ldx, nch, n = C.c_long(), C.c_int(), C.c_long()
+        p = lib().txo_sp_block(self.h, C.byref(ldx), C.byref(nch), C.byref(n))
+        a = np.ctypeslib.as_array(p, shape=(nch.value, ldx.value))
+        return a[:, : n.value].copy()
+
+    def zap_ranges(self, irfi):
+        nrows = C.c_int()
+        p = lib().txo_sp_zap_ranges(self.h, irfi, C.byref(nrows))
+        if not p:
+            return None
+        return np.ctypeslib.as_array(p, shape=(nrows.value, 4)).copy()
+
+    def timdata(self):
+        i = self.info()
+        return np.ctypeslib.as_array(lib().txo_sp_timdata(self.h), shape=(i.ndm, i.nout)).copy()
+
+    def mxS(self):
+        i = self.info()
+        return np.ctypeslib.as_array(lib().txo_sp_mxS(self.h), shape=(i.ndm, i.nout)).copy()
+
+    def mxwn(self):
+        i = self.info()
+        return np.ctypeslib.as_array(lib().txo_sp_mxwn(self.h), shape=(i.ndm, i.nout)).copy()
+
+    def freqs(self):
+        i = self.info()
+        out = np.zeros(i.nchan, np.float64)
+        lib().txo_sp_freqs(self.h, out)
+        return out
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().txo_sp_destroy(self.h)
+            self.h = None
+
+
+# ---- the reference's own code, compiled in place (only where the reference tree exists) -----
+
+_ref = {}
+
+
+def ref_available(variant="scalar") -> bool:
+    return os.path.exists(os.path.join(HERE, "_ref", f"libtxref_{variant}.so"))
+
+
+def ref_lib(variant="scalar") -> C.CDLL:
+    if variant in _ref:
+        return _ref[variant]
+    L = C.CDLL(os.path.join(HERE, "_ref", f"libtxref_{variant}.so"))
+    L.ref_boxcar_run.restype = C.c_int
+    L.ref_boxcar_run.argtypes = [f32p, C.c_long, C.c_long, i32p, C.c_int, C.c_int, f32p, i32p,
+                                 C.c_int]
+    L.ref_cluster_run.restype = C.c_long
+    L.ref_cluster_run.argtypes = [f32p, i32p, C.c_long, C.c_long, C.c_double, C.c_double,
+                                  C.c_double, C.c_double, C.c_double, C.c_int, C.c_float,
+                                  C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_long,
+                                  i64p, i64p, i32p, f32p, C.c_long]
+    _ref[variant] = L
+    return L
+
+
+def ref_boxcar_run(tim, vwn, iqr=False, variant="scalar", nthreads=4):
+    tim = np.ascontiguousarray(tim, np.float32)
+    ndm, n = tim.shape
+    vwn = np.ascontiguousarray(vwn, np.int32)
+    mxS = np.zeros((ndm, n), np.float32)
+    mxwn = np.zeros((ndm, n), np.int32)
+    ref_lib(variant).ref_boxcar_run(tim, ndm, n, vwn, len(vwn), int(iqr), mxS, mxwn, nthreads)
+    return mxS, mxwn
+
+
+def ref_cluster_run(mxS, mxwn, dms, ddm, tsamp, fmin, fmax, maxwn, thre, radius, kvalue,
+                    maxncand, minpts, drop, counter=1, variant="scalar"):
+    mxS = np.ascontiguousarray(mxS, np.float32)
+    mxwn = np.ascontiguousarray(mxwn, np.int32)
+    ndm, n = mxS.shape
+    cap = max(int(maxncand), 1)
+    idm = np.zeros(cap, np.int64)
+    isamp = np.zeros(cap, np.int64)
+    wn = np.zeros(cap, np.int32)
+    S = np.zeros(cap, np.float32)
+    m = ref_lib(variant).ref_cluster_run(mxS, mxwn, ndm, n, dms, ddm, tsamp, fmin, fmax, maxwn,
+                                         thre, radius, kvalue, maxncand, minpts, int(drop),
+                                         counter, idm, isamp, wn, S, cap)
+    out = np.zeros(max(m, 0), CAND_DTYPE)
+    out["idm"], out["isamp"], out["wn"], out["S"] = idm[:m], isamp[:m], wn[:m], S[:m]
+    return out

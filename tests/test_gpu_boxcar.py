@@ -1,0 +1,61 @@
+"""GPU boxcar (txg_boxcar, the Boxcar::run boundary) against the oracle and the reference's
+golden outputs."""
+import numpy as np
+import pytest
+
+from gpu_util import assert_boxcar_close, assert_cands_close
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("var", ["scalar", "avx2"])
+def test_boxcar_golden(tx, golden, var):
+    g = golden["boxcar"]
+    if f"mxS_{var}_iqr0" not in g:
+        pytest.skip("variant not in fixture")
+    for iqr in (0, 1):
+        S, W, c = tx.boxcar(g["tim"], g["vwn"], iqr=bool(iqr), avx2_tail=var == "avx2", thre=7.0)
+        assert_boxcar_close(g["tim"], g["vwn"], S, W, g[f"mxS_{var}_iqr{iqr}"],
+                            g[f"mxwn_{var}_iqr{iqr}"], iqr=bool(iqr))
+
+
+@pytest.mark.parametrize("n", [17, 1000, 4097, 15625, 40000])
+def test_boxcar_random_vs_oracle(tx, oracle, n):
+    rng = np.random.default_rng(n)
+    ndm = 12
+    tim = rng.normal(0, 20, (ndm, n)).astype(np.float32)
+    tim[0, n // 3: n // 3 + 5] += 300
+    tim[3] = 1.0
+    vwn = oracle.width_ladder(1e-4, 0.05, 0.1, 64e-6)
+    vwn = vwn[vwn < max(3, n // 2)]
+    for iqr in (False, True):
+        for avx in (False, True):
+            Sr, Wr = oracle.boxcar_run(tim, vwn, iqr, avx)
+            S, W, c = tx.boxcar(tim, vwn, iqr=iqr, avx2_tail=avx, thre=4.0)
+            assert_boxcar_close(tim, vwn, S, W, Sr, Wr, iqr=iqr)
+            assert_cands_close(c, oracle.threshold_scan(Sr, Wr, 4.0), 4.0)
+
+
+def test_boxcar_candidates_only(tx, oracle):
+    rng = np.random.default_rng(7)
+    tim = rng.normal(0, 1, (40, 3000)).astype(np.float32)
+    tim[10:14, 1500:1510] += 6
+    vwn = oracle.width_ladder(1e-4, 0.02, 0.1, 1e-4)
+    _, _, c = tx.boxcar(tim, vwn, thre=6.0, dense=False)
+    Sr, Wr = oracle.boxcar_run(tim, vwn)
+    assert_cands_close(c, oracle.threshold_scan(Sr, Wr, 6.0), 6.0)
+    assert len(c) > 0
+
+
+def test_boxcar_overflow_reported(tx):
+    tim = np.zeros((4, 1000), np.float32)
+    tim[:, ::2] = 50.0
+    with pytest.raises(tx.TxgError) as e:
+        tx.boxcar(tim, [1, 2], thre=0.1, cand_capacity=10)
+    assert e.value.status == tx.ERR_OVERFLOW
+
+
+def test_boxcar_rejects_bad_arguments(tx):
+    with pytest.raises(tx.TxgError) as e:
+        tx.boxcar(np.zeros((2, 10), np.float32), [])
+    assert e.value.status == tx.ERR_ARG

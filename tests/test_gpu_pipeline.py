@@ -1,0 +1,144 @@
+"""Full per-block chain on the GPU (txg_create / txg_push_block) against the oracle's
+SinglePulse::run restatement, block by block: preprocessed data and kadaneF windows
+bit-exact, dedispersed series bit-exact on the FP32 path, boxcar S within 1e-4."""
+import numpy as np
+import pytest
+
+from gpu_util import assert_boxcar_close, assert_cands_close
+
+pytestmark = pytest.mark.gpu
+
+
+def small_workload(seed=21, nsamples=4096 * 6):
+    from transientx_gb300 import SinglePulse, synth
+    tsamp, C = 256e-6, 128
+    f = synth.band(C, 1500.0, 1200.0)
+    rng = np.random.default_rng(seed)
+    T = nsamples * tsamp
+    sines = [(int(c), float(rng.uniform(10, 30)), float(rng.uniform(0.02, 0.2)), 0.3)
+             for c in rng.choice(C, 6, replace=False)]
+    imps = [(float(rng.uniform(0, T)), int(rng.integers(1, 20)), 20.0) for _ in range(3)]
+    pulses = [(0.3 * T, 60.0, 3e-3, 25.0), (0.55 * T, 150.0, 1e-3, 15.0),
+              (0.75 * T, 300.0, 8e-3, 30.0)]
+    fil = synth.Filterbank(C, tsamp, f, nsamples, seed, pulses=pulses, sines=sines, impulses=imps)
+    rfi = [["kadaneF", "8", "4"], ["zdot"]]
+    rows = [SinglePulse(td=1, fd=1, dms=0.0, ddm=1.0, ndm=200, maxw=0.05, rfilist=rfi,
+                        widthlimit=0.02, bswidth=0.1, nsub=16),
+            SinglePulse(td=2, fd=2, dms=200.0, ddm=2.0, ndm=100, maxw=0.05, rfilist=rfi,
+                        widthlimit=0.02, bswidth=0.0, nsub=8, overlap=0.1)]
+    return fil, rows, 4096
+
+
+def oracle_rows(oracle, rows, fil, ndump, tx, avx2=False):
+    out = []
+    for r, sp in enumerate(rows):
+        info = tx.describe_row(rows, r, fil.nchans, fil.tsamp, fil.freqs, ndump)[0]
+        row = oracle.make_row(td=sp.td, fd=sp.fd, bswidth=sp.bswidth, rfi=sp.rfilist,
+                              threKadaneF=sp.threKadaneF, widthlimit=sp.widthlimit, dms=sp.dms,
+                              ddm=sp.ddm, ndm=sp.ndm, overlap=sp.overlap, nsub=info.nsub,
+                              group=info.dm_group, minw=sp.minw, maxw=sp.maxw,
+                              snrloss=sp.snrloss, iqr=sp.iqr, thre=sp.thre, avx2_tail=avx2)
+        out.append(oracle.SinglePulseRow(row, fil.freqs, fil.tsamp, ndump))
+    return out
+
+
+@pytest.mark.parametrize("avx2", [False, True])
+def test_pipeline_fp32_matches_oracle(tx, oracle, avx2):
+    fil, rows, ndump = small_workload()
+    flags = tx.FLAG_DENSE | tx.FLAG_KEEP_SERIES | (tx.FLAG_AVX2_TAIL if avx2 else 0)
+    orows = oracle_rows(oracle, rows, fil, ndump, tx, avx2)
+    nblk = fil.nsamples // ndump
+    ngated = 0
+    with tx.Search(rows, fil.nchans, fil.tsamp, fil.freqs, ndump, flags=flags) as s:
+        for b in range(nblk):
+            raw = fil.generate(b * ndump, ndump)
+            s.push_block(raw)
+            s.sync()
+            for r, o in enumerate(orows):
+                gated = o.run(raw)
+                info = s.row_info(r)
+                assert bool(info.gated) == gated and info.counter == o.info().counter
+                np.testing.assert_array_equal(s.block(r), o.block(), err_msg=f"block {b} row {r}")
+                zr = s.zap_ranges(0, r)
+                np.testing.assert_array_equal(zr, o.zap_ranges(0))
+                if not gated:
+                    continue
+                ngated += 1
+                tim = s.timdata(r)
+                np.testing.assert_array_equal(tim, o.timdata(), err_msg=f"tim block {b} row {r}")
+                S, W = s.dense(r)
+                vwn = o.widths()
+                assert_boxcar_close(tim, vwn, S, W, o.mxS(), o.mxwn())
+                ref = oracle.threshold_scan(o.mxS(), o.mxwn(), rows[r].thre)
+                assert_cands_close(s.candidates(r), ref, rows[r].thre)
+    assert ngated >= 4
+
+
+def test_kadane_fires_on_rfi(tx, oracle):
+    fil, rows, ndump = small_workload()
+    with tx.Search(rows[:1], fil.nchans, fil.tsamp, fil.freqs, ndump,
+                   flags=tx.FLAG_KEEP_SERIES) as s:
+        s.push_block(fil.generate(0, ndump))
+        s.sync()
+        zr = s.zap_ranges(0)
+    assert (zr[:, 0] >= 0).any(), "the sinusoid channels should be zapped"
+
+
+@pytest.mark.parametrize("prec,bound", [("fp16", 4e-3), ("bf16", 3e-2)])
+def test_reduced_precision_series(tx, prec, bound):
+    """BF16/FP16 storage of the subband series: dedispersed series stay close to FP32.  Each
+    stored subband sample carries a relative rounding error of at most 2^-9 (bf16) or 2^-12
+    (fp16); summed over 8-16 subbands that bounds the worst sample at a few percent (bf16) or
+    a few 1e-3 (fp16) of the series' standard deviation."""
+    fil, rows, ndump = small_workload()
+    flags = tx.FLAG_KEEP_SERIES
+    with tx.Search(rows, fil.nchans, fil.tsamp, fil.freqs, ndump, flags=flags) as a, \
+            tx.Search(rows, fil.nchans, fil.tsamp, fil.freqs, ndump, flags=flags,
+                      precision=prec) as b:
+        for blk in range(4):
+            raw = fil.generate(blk * ndump, ndump)
+            a.push_block(raw)
+            b.push_block(raw)
+        a.sync()
+        b.sync()
+        for r in range(len(rows)):
+            ta, tb = a.timdata(r), b.timdata(r)
+            scale = ta.std(axis=1, keepdims=True)
+            err = np.abs(ta - tb) / scale
+            assert err.max() < bound, (prec, r, err.max())
+
+
+def test_candidate_overflow_is_reported(tx):
+    fil, rows, ndump = small_workload()
+    rows = [rows[0]]
+    rows[0].thre = -1e9  # every point passes
+    with tx.Search(rows, fil.nchans, fil.tsamp, fil.freqs, ndump, cand_capacity=1000) as s:
+        for blk in range(3):
+            s.push_block(fil.generate(blk * ndump, ndump))
+        rc = s.sync(allow_overflow=True)
+        assert rc == tx.ERR_OVERFLOW
+        assert len(s.candidates(0)) == 1000
+
+
+def test_device_pointer_input_matches_host_input(tx):
+    import ctypes
+    fil, rows, ndump = small_workload()
+    cudart = ctypes.CDLL("libcudart.so")
+    raw = fil.generate(0, 3 * ndump)
+    dptr = ctypes.c_void_p()
+    assert cudart.cudaMalloc(ctypes.byref(dptr), ctypes.c_size_t(raw.nbytes)) == 0
+    try:
+        assert cudart.cudaMemcpy(dptr, raw.ctypes.data, ctypes.c_size_t(raw.nbytes), 1) == 0
+        with tx.Search(rows, fil.nchans, fil.tsamp, fil.freqs, ndump,
+                       flags=tx.FLAG_KEEP_SERIES) as a, \
+                tx.Search(rows, fil.nchans, fil.tsamp, fil.freqs, ndump,
+                          flags=tx.FLAG_KEEP_SERIES) as b:
+            for blk in range(3):
+                a.push_block(raw[blk * ndump:(blk + 1) * ndump])
+                b.push_block_device(dptr.value + blk * ndump * fil.nchans)
+            a.sync()
+            b.sync()
+            for r in range(len(rows)):
+                np.testing.assert_array_equal(a.timdata(r), b.timdata(r))
+    finally:
+        cudart.cudaFree(dptr)

@@ -1,0 +1,447 @@
+"""transientx_gb300 -- GB300 (sm_103a) implementation of TransientX's per-block single-pulse
+search, driven through the C ABI of include/transientx_gb300.h.
+
+The Python layer mirrors the reference's host interface for this path:
+  * ``SinglePulse`` carries the per-ddplan-row configuration members of the reference class
+    (include/singlepulse.h:95-133) and ``parse_ddplan`` reads the ddplan text format of
+    parse() (src/singlepulse/singlepulse.cpp:407-463);
+  * ``Search`` owns one handle: ``push_block`` is one iteration of the transientx_fil block
+    loop (dedisperse_fil.cpp:319-337) over all ddplan rows, ``candidates`` yields the
+    S > thre points Cluster::run consumes, ``cluster`` runs the clustering;
+  * ``boxcar`` is Boxcar::run over caller-supplied dedispersed series.
+All compute runs in the CUDA library; importing this module without it raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+from typing import List, Optional, Sequence, Tuple
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libtxgpu.so")
+
+OK = 0
+ERR_ARG, ERR_NOMEM, ERR_CUDA, ERR_OVERFLOW = -1, -2, -3, -4
+ERR_TIMEOUT, ERR_STATE, ERR_NODEVICE, ERR_UNSUPPORTED = -5, -6, -7, -8
+RFI_KADANEF, RFI_ZDOT = 1, 2
+PREC_FP32, PREC_BF16, PREC_FP16 = 0, 1, 2
+FLAG_AVX2_TAIL, FLAG_DENSE, FLAG_KEEP_SERIES, FLAG_TIMING = 1, 2, 4, 8
+PRECISIONS = {"fp32": PREC_FP32, "bf16": PREC_BF16, "fp16": PREC_FP16}
+
+
+class TxgError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(msg)
+        self.status = status
+
+
+class txg_row(C.Structure):
+    _fields_ = [
+        ("td", C.c_int32), ("fd", C.c_int32), ("bswidth", C.c_float), ("nrfi", C.c_int32),
+        ("rfi_kind", C.c_int32 * 8), ("rfi_td", C.c_int32 * 8), ("rfi_fd", C.c_int32 * 8),
+        ("nzap", C.c_int32), ("zap", (C.c_double * 2) * 16), ("threKadaneF", C.c_float),
+        ("widthlimit", C.c_double), ("dms", C.c_double), ("ddm", C.c_double),
+        ("ndm", C.c_int64), ("overlap", C.c_double), ("minw", C.c_float), ("maxw", C.c_float),
+        ("snrloss", C.c_float), ("iqr", C.c_int32), ("thre", C.c_float), ("nsub", C.c_int32),
+        ("dm_group", C.c_int32),
+    ]
+
+
+class txg_plan(C.Structure):
+    _fields_ = [
+        ("nchans", C.c_int32), ("tsamp", C.c_double), ("frequencies", C.POINTER(C.c_double)),
+        ("ndump", C.c_int64), ("nrows", C.c_int32), ("rows", C.POINTER(txg_row)),
+        ("nbeams", C.c_int32), ("precision", C.c_int32), ("flags", C.c_int32),
+        ("cand_capacity", C.c_int64),
+    ]
+
+
+class txg_row_info(C.Structure):
+    _fields_ = [
+        ("nchans", C.c_int32), ("nsub", C.c_int32), ("dm_group", C.c_int32),
+        ("ngroup", C.c_int32), ("nwidths", C.c_int32), ("maxwn", C.c_int32),
+        ("ndm", C.c_int64), ("ndump", C.c_int64), ("noverlap", C.c_int64), ("offset", C.c_int64),
+        ("nsamples", C.c_int64), ("counter", C.c_int64), ("maxd1", C.c_int64),
+        ("maxd2", C.c_int64), ("tsamp", C.c_double), ("dms", C.c_double), ("ddm", C.c_double),
+        ("fmin", C.c_double), ("fmax", C.c_double), ("gated", C.c_int32), ("pad", C.c_int32),
+    ]
+
+
+CAND_DTYPE = np.dtype([("idm", "<i4"), ("isamp", "<i4"), ("wn", "<i4"), ("S", "<f4")])
+
+# every symbol include/transientx_gb300.h declares
+EXPORTS = [
+    "txg_create", "txg_destroy", "txg_push_block", "txg_push_block_device", "txg_sync",
+    "txg_get_row_info", "txg_get_candidates", "txg_get_dense", "txg_get_timdata",
+    "txg_get_block", "txg_get_zap_ranges", "txg_get_tables", "txg_width_ladder", "txg_boxcar",
+    "txg_cluster", "txg_get_timing", "txg_get_stream", "txg_strerror", "txg_version",
+    "txg_describe_row", "txg_pop_result",
+]
+
+_lib: Optional[C.CDLL] = None
+vp = C.c_void_p
+
+
+def load_library(path: str = LIB_PATH) -> C.CDLL:
+    """Load the CUDA library (built in-tree by ``transientx_gb300._build``)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: build it with `python -m transientx_gb300._build` "
+                          "(there is no CPU fallback)")
+    L = C.CDLL(path)
+    L.txg_version.restype = C.c_int32
+    L.txg_strerror.restype = C.c_char_p
+    L.txg_strerror.argtypes = [C.c_int32]
+    L.txg_create.argtypes = [C.POINTER(txg_plan), C.POINTER(vp)]
+    L.txg_destroy.argtypes = [vp]
+    L.txg_destroy.restype = None
+    L.txg_push_block.argtypes = [vp, C.c_int32, vp, C.c_int64]
+    L.txg_push_block_device.argtypes = [vp, C.c_int32, vp, C.c_int64]
+    L.txg_sync.argtypes = [vp]
+    L.txg_get_row_info.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(txg_row_info)]
+    L.txg_get_candidates.argtypes = [vp, C.c_int32, C.c_int32, vp, C.c_int64,
+                                     C.POINTER(C.c_int64)]
+    L.txg_get_dense.argtypes = [vp, C.c_int32, C.c_int32, vp, vp]
+    L.txg_get_timdata.argtypes = [vp, C.c_int32, C.c_int32, C.c_int64, C.c_int64, vp]
+    L.txg_get_block.argtypes = [vp, C.c_int32, C.c_int32, vp]
+    L.txg_get_zap_ranges.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, vp, C.c_int64]
+    L.txg_get_tables.argtypes = [vp, C.c_int32, vp, vp, vp, vp]
+    L.txg_width_ladder.argtypes = [C.c_float, C.c_float, C.c_float, C.c_double, vp, C.c_int32]
+    L.txg_boxcar.argtypes = [vp, C.c_int64, C.c_int64, vp, C.c_int32, C.c_int32, C.c_int32,
+                             C.c_float, vp, vp, vp, C.c_int64, C.POINTER(C.c_int64)]
+    L.txg_cluster.argtypes = [vp, C.c_int64, C.c_double, C.c_double, C.c_double, C.c_double,
+                              C.c_double, C.c_double, C.c_int32, C.c_int32, C.c_int32,
+                              C.c_int32, vp, C.c_int64, C.POINTER(C.c_int64)]
+    L.txg_get_timing.argtypes = [vp, vp, vp, C.c_int32]
+    L.txg_get_stream.argtypes = [vp, C.POINTER(vp)]
+    L.txg_pop_result.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(C.c_int64),
+                                 C.POINTER(C.c_int32), vp, C.c_int64, C.POINTER(C.c_int64)]
+    L.txg_describe_row.argtypes = [C.POINTER(txg_plan), C.c_int32, C.POINTER(txg_row_info), vp,
+                                   vp, vp, vp]
+    _lib = L
+    return L
+
+
+def _check(rc: int, what: str = "") -> None:
+    if rc != OK:
+        msg = load_library().txg_strerror(rc).decode()
+        raise TxgError(rc, f"{what}: {msg}" if what else msg)
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+# ---- configuration mirror --------------------------------------------------------------
+
+@dataclass
+class SinglePulse:
+    """Configuration of one ddplan row, with the member names of the reference's SinglePulse
+    (include/singlepulse.h:95-133) and its defaults (src/singlepulse/singlepulse.cpp:18-65,
+    CLI defaults of src/singlepulse/dedisperse_fil.cpp:54-99 where the CLI sets them)."""
+    td: int = 1
+    fd: int = 1
+    bswidth: float = 0.1
+    zaplist: List[Tuple[float, float]] = field(default_factory=list)
+    rfilist: List[List[str]] = field(default_factory=list)
+    widthlimit: float = 50e-3
+    threKadaneF: float = 7.0
+    dms: float = 0.0
+    ddm: float = 1.0
+    ndm: int = 200
+    overlap: float = 0.0
+    minw: float = 1e-4
+    maxw: float = 0.02
+    snrloss: float = 0.1
+    iqr: bool = False
+    thre: float = 7.0
+    radius_smearing: float = 1e-3
+    kvalue: int = 2
+    maxncand: int = 100
+    minpts: int = 5
+    remove_cand_with_maxwidth: bool = False
+    nsub: int = 0
+    dm_group: int = 0
+    id: int = 1
+
+    def to_c(self) -> txg_row:
+        r = txg_row()
+        r.td, r.fd, r.bswidth = self.td, self.fd, self.bswidth
+        if len(self.rfilist) > 8 or len(self.zaplist) > 16:
+            raise ValueError("at most 8 rfilist and 16 zaplist entries")
+        r.nrfi = len(self.rfilist)
+        for i, op in enumerate(self.rfilist):
+            if op[0] == "kadaneF":
+                r.rfi_kind[i], r.rfi_td[i], r.rfi_fd[i] = RFI_KADANEF, int(op[1]), int(op[2])
+            elif op[0] == "zdot":
+                r.rfi_kind[i], r.rfi_td[i], r.rfi_fd[i] = RFI_ZDOT, 1, 1
+            else:
+                raise TxgError(ERR_UNSUPPORTED, f"rfilist entry {op[0]!r} is not implemented")
+        r.nzap = len(self.zaplist)
+        for i, (a, b) in enumerate(self.zaplist):
+            r.zap[i][0], r.zap[i][1] = a, b
+        r.threKadaneF, r.widthlimit = self.threKadaneF, self.widthlimit
+        r.dms, r.ddm, r.ndm, r.overlap = self.dms, self.ddm, self.ndm, self.overlap
+        r.minw, r.maxw, r.snrloss = self.minw, self.maxw, self.snrloss
+        r.iqr, r.thre = int(self.iqr), self.thre
+        r.nsub, r.dm_group = self.nsub, self.dm_group
+        return r
+
+
+def _rfi_opts(tokens: Sequence[str], sp: SinglePulse) -> None:
+    i = 0
+    while i < len(tokens):
+        t = tokens[i]
+        if t in ("mask", "kadaneF", "kadaneT"):
+            sp.rfilist.append([t, tokens[i + 1], tokens[i + 2]])
+            i += 3
+        elif t == "zap":
+            sp.zaplist.append((float(tokens[i + 1]), float(tokens[i + 2])))
+            i += 3
+        elif t in ("zero", "zdot"):
+            sp.rfilist.append([t])
+            i += 1
+        else:
+            i += 1
+
+
+def parse_ddplan(text: str, base: Optional[SinglePulse] = None) -> List[SinglePulse]:
+    """ddplan rows ``td fd dms ddm ndm snrloss maxw [rfi options]``; lines not starting with a
+    digit are skipped and each row inherits the rfi options of earlier rows, as parse() does
+    (singlepulse.cpp:407-456)."""
+    import copy
+    sp = copy.deepcopy(base) if base is not None else SinglePulse()
+    rows, ident = [], 0
+    for line in text.splitlines():
+        line = line.strip()
+        if not line or not line[0].isdigit():
+            continue
+        p = line.split()
+        sp.td, sp.fd = int(p[0]), int(p[1])
+        sp.dms, sp.ddm, sp.ndm = float(p[2]), float(p[3]), int(p[4])
+        sp.snrloss, sp.maxw = float(p[5]), float(p[6])
+        _rfi_opts(p[7:], sp)
+        ident += 1
+        sp.id = ident
+        rows.append(copy.deepcopy(sp))
+    return rows
+
+
+def width_ladder(minw: float, maxw: float, snrloss: float, tsamp: float) -> np.ndarray:
+    out = np.zeros(256, np.int32)
+    n = load_library().txg_width_ladder(minw, maxw, snrloss, tsamp, _ptr(out), 256)
+    return out[:n].copy()
+
+
+def _make_plan(rows, nchans, tsamp, freqs, ndump, nbeams, precision, flags, cand_capacity):
+    crows = (txg_row * len(rows))(*[r.to_c() for r in rows])
+    plan = txg_plan()
+    plan.nchans, plan.tsamp = nchans, tsamp
+    plan.frequencies = freqs.ctypes.data_as(C.POINTER(C.c_double))
+    plan.ndump, plan.nrows, plan.rows = ndump, len(rows), crows
+    plan.nbeams, plan.precision, plan.flags = nbeams, PRECISIONS[precision], flags
+    plan.cand_capacity = cand_capacity
+    return plan, crows
+
+
+def describe_row(rows: Sequence[SinglePulse], row: int, nchans: int, tsamp: float,
+                 frequencies: Sequence[float], ndump: int):
+    """Host-only planning of one ddplan row: (info, d1, d2, sub_start, vwn)."""
+    freqs = np.ascontiguousarray(frequencies, np.float64)
+    plan, crows = _make_plan(rows, nchans, tsamp, freqs, ndump, 1, "fp32", 0, 0)
+    info = txg_row_info()
+    L = load_library()
+    _check(L.txg_describe_row(C.byref(plan), row, C.byref(info), None, None, None, None),
+           "describe_row")
+    d1 = np.zeros((info.ngroup, info.nchans), np.int32)
+    d2 = np.zeros((info.ndm, info.nsub), np.int32)
+    ss = np.zeros(info.nsub + 1, np.int32)
+    vwn = np.zeros(info.nwidths, np.int32)
+    _check(L.txg_describe_row(C.byref(plan), row, C.byref(info), _ptr(d1), _ptr(d2), _ptr(ss),
+                              _ptr(vwn)), "describe_row")
+    return info, d1, d2, ss, vwn
+
+
+# ---- handle ------------------------------------------------------------------------------
+
+class Search:
+    """One handle: all ddplan rows of ``rows`` for ``nbeams`` beams of the same format."""
+
+    def __init__(self, rows: Sequence[SinglePulse], nchans: int, tsamp: float,
+                 frequencies: Sequence[float], ndump: int, nbeams: int = 1,
+                 precision: str = "fp32", flags: int = 0, cand_capacity: int = 0):
+        L = load_library()
+        self.rows = list(rows)
+        self.nchans, self.tsamp, self.ndump, self.nbeams = nchans, tsamp, ndump, nbeams
+        self._freqs = np.ascontiguousarray(frequencies, np.float64)
+        if len(self._freqs) != nchans:
+            raise ValueError("need one frequency per channel")
+        plan, self._crows = _make_plan(self.rows, nchans, tsamp, self._freqs, ndump, nbeams,
+                                       precision, flags, cand_capacity)
+        self.cap = cand_capacity if cand_capacity > 0 else 1 << 20
+        self.flags = flags
+        h = vp()
+        _check(L.txg_create(C.byref(plan), C.byref(h)), "txg_create")
+        self.h = h
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            load_library().txg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def push_block(self, raw: np.ndarray, beam: int = 0) -> None:
+        raw = np.ascontiguousarray(raw, np.uint8)
+        if raw.shape != (self.ndump, self.nchans):
+            raise ValueError(f"block must be [{self.ndump}][{self.nchans}] uint8")
+        rc = load_library().txg_push_block(self.h, beam, _ptr(raw), self.ndump)
+        if rc not in (OK, ERR_OVERFLOW):
+            _check(rc, "txg_push_block")
+
+    def push_block_device(self, dev_ptr: int, beam: int = 0) -> None:
+        rc = load_library().txg_push_block_device(self.h, beam, int(dev_ptr), self.ndump)
+        if rc not in (OK, ERR_OVERFLOW):
+            _check(rc, "txg_push_block_device")
+
+    def sync(self, allow_overflow: bool = False) -> int:
+        rc = load_library().txg_sync(self.h)
+        if rc == ERR_OVERFLOW and allow_overflow:
+            return rc
+        _check(rc, "txg_sync")
+        return rc
+
+    def row_info(self, row: int = 0, beam: int = 0) -> txg_row_info:
+        info = txg_row_info()
+        _check(load_library().txg_get_row_info(self.h, beam, row, C.byref(info)), "row_info")
+        return info
+
+    def candidates(self, row: int = 0, beam: int = 0) -> np.ndarray:
+        L = load_library()
+        n = C.c_int64()
+        L.txg_get_candidates(self.h, beam, row, None, 0, C.byref(n))
+        kept = min(n.value, self.cap)
+        out = np.zeros(kept, CAND_DTYPE)
+        rc = L.txg_get_candidates(self.h, beam, row, _ptr(out), kept, C.byref(n))
+        if rc not in (OK, ERR_OVERFLOW):
+            _check(rc, "candidates")
+        return out
+
+    def pop_result(self, row: int = 0, beam: int = 0):
+        """Oldest unread block of (beam,row): (counter, gated, candidates) or None."""
+        L = load_library()
+        cnt, gated, n = C.c_int64(), C.c_int32(), C.c_int64()
+        buf = getattr(self, "_popbuf", None)
+        if buf is None:
+            buf = self._popbuf = np.zeros(self.cap, CAND_DTYPE)
+        rc = L.txg_pop_result(self.h, beam, row, C.byref(cnt), C.byref(gated), _ptr(buf),
+                              len(buf), C.byref(n))
+        if rc == ERR_STATE:
+            return None
+        if rc not in (OK, ERR_OVERFLOW):
+            _check(rc, "pop_result")
+        m = min(n.value, self.cap)
+        return cnt.value, bool(gated.value), buf[:m].copy(), n.value
+
+    def dense(self, row: int = 0, beam: int = 0) -> Tuple[np.ndarray, np.ndarray]:
+        i = self.row_info(row, beam)
+        mxS = np.zeros((i.ndm, i.nsamples), np.float32)
+        mxwn = np.zeros((i.ndm, i.nsamples), np.int32)
+        _check(load_library().txg_get_dense(self.h, beam, row, _ptr(mxS), _ptr(mxwn)), "dense")
+        return mxS, mxwn
+
+    def timdata(self, row: int = 0, beam: int = 0, idm0: int = 0, count: int = -1) -> np.ndarray:
+        i = self.row_info(row, beam)
+        count = i.ndm - idm0 if count < 0 else count
+        out = np.zeros((count, i.nsamples), np.float32)
+        _check(load_library().txg_get_timdata(self.h, beam, row, idm0, count, _ptr(out)),
+               "timdata")
+        return out
+
+    def block(self, row: int = 0, beam: int = 0) -> np.ndarray:
+        i = self.row_info(row, beam)
+        out = np.zeros((i.nchans, i.ndump), np.float32)
+        _check(load_library().txg_get_block(self.h, beam, row, _ptr(out)), "block")
+        return out
+
+    def zap_ranges(self, irfi: int, row: int = 0, beam: int = 0) -> np.ndarray:
+        i = self.row_info(row, beam)
+        fd = int(self.rows[row].rfilist[irfi][2])
+        out = np.zeros((i.nchans // fd, 4), np.int32)
+        _check(load_library().txg_get_zap_ranges(self.h, beam, row, irfi, _ptr(out), out.size),
+               "zap_ranges")
+        return out
+
+    def tables(self, row: int = 0):
+        i = self.row_info(row)
+        d1 = np.zeros((i.ngroup, i.nchans), np.int32)
+        d2 = np.zeros((i.ndm, i.nsub), np.int32)
+        ss = np.zeros(i.nsub + 1, np.int32)
+        vwn = np.zeros(i.nwidths, np.int32)
+        _check(load_library().txg_get_tables(self.h, row, _ptr(d1), _ptr(d2), _ptr(ss),
+                                             _ptr(vwn)), "tables")
+        return d1, d2, ss, vwn
+
+    def timing(self) -> Tuple[np.ndarray, np.ndarray]:
+        ms = np.zeros(8, np.float64)
+        n = np.zeros(8, np.int64)
+        k = load_library().txg_get_timing(self.h, _ptr(ms), _ptr(n), 8)
+        return ms[:k], n[:k]
+
+    def stream(self) -> int:
+        s = vp()
+        _check(load_library().txg_get_stream(self.h, C.byref(s)), "stream")
+        return s.value or 0
+
+    def cluster(self, row: int = 0, beam: int = 0, cands: Optional[np.ndarray] = None):
+        """Cluster<double>::run on this row's last block (cluster.cpp:63-161)."""
+        sp = self.rows[row]
+        i = self.row_info(row, beam)
+        if cands is None:
+            cands = self.candidates(row, beam)
+        return cluster(cands, i.dms, i.ddm, i.fmax, i.fmin, i.tsamp, sp.radius_smearing,
+                       sp.maxncand, sp.minpts, sp.remove_cand_with_maxwidth, i.maxwn)
+
+
+def boxcar(tim: np.ndarray, vwn: Sequence[int], iqr: bool = False, avx2_tail: bool = False,
+           thre: float = 7.0, dense: bool = True, cand_capacity: int = 1 << 20):
+    """Boxcar::run (boxcar.cpp:158-296) on the GPU over caller-supplied series [ndm][n]."""
+    tim = np.ascontiguousarray(tim, np.float32)
+    ndm, n = tim.shape
+    vwn = np.ascontiguousarray(vwn, np.int32)
+    mxS = np.zeros((ndm, n), np.float32) if dense else None
+    mxwn = np.zeros((ndm, n), np.int32) if dense else None
+    cands = np.zeros(cand_capacity, CAND_DTYPE)
+    nc = C.c_int64()
+    rc = load_library().txg_boxcar(_ptr(tim), ndm, n, _ptr(vwn), len(vwn), int(iqr),
+                                   FLAG_AVX2_TAIL if avx2_tail else 0, thre,
+                                   _ptr(mxS) if dense else None, _ptr(mxwn) if dense else None,
+                                   _ptr(cands), cand_capacity, C.byref(nc))
+    _check(rc, "txg_boxcar")
+    return mxS, mxwn, cands[: nc.value].copy()
+
+
+def cluster(cands: np.ndarray, dms: float, ddm: float, fmax: float, fmin: float, tsamp: float,
+            radius_smearing: float, maxncand: int, minpts: int, drop: bool,
+            maxwn: int) -> np.ndarray:
+    """Cluster<double>::run (cluster.cpp:63-161): the reported (idm, isamp, wn, S) list."""
+    cands = np.ascontiguousarray(cands, CAND_DTYPE)
+    out = np.zeros(max(maxncand, 1), CAND_DTYPE)
+    n = C.c_int64()
+    _check(load_library().txg_cluster(_ptr(cands) if len(cands) else None, len(cands), dms, ddm,
+                                      fmax, fmin, tsamp, radius_smearing, maxncand, minpts,
+                                      int(drop), maxwn, _ptr(out), len(out), C.byref(n)),
+           "txg_cluster")
+    return out[: n.value].copy()

@@ -1,0 +1,823 @@
+/*
+ * txg_api.cu -- the extern "C" boundary (include/transientx_gb300.h): plan, device state,
+ * per-block launch sequence and candidate harvesting.
+ *
+ * Per pushed block and ddplan row, on the handle's stream (SinglePulse::run order,
+ * src/singlepulse/singlepulse.cpp:287-341):
+ *   history copy -> unpack+downsample -> equalize -> baseline -> zap -> rfilist ops ->
+ *   stage 1 (ring) -> [gate, boxcar.cpp:161] stage 2 -> boxcar+threshold -> async D2H.
+ * Candidate buffers rotate over NSLOT slots per (beam,row) so the device runs ahead of the
+ * host; a slot is harvested (sorted into Cluster::run order, cluster.cpp:91-112) before it
+ * is reused and at txg_sync.
+ */
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <string>
+#include <vector>
+
+#include "txg_internal.h"
+
+namespace txg {
+
+static thread_local std::string g_err;
+
+int set_cuda_error(cudaError_t e, const char *expr, const char *file, int line)
+{
+    char buf[512];
+    snprintf(buf, sizeof(buf), "%s failed: %s (%s:%d)", expr, cudaGetErrorString(e), file, line);
+    g_err = buf;
+    if (e == cudaErrorMemoryAllocation) return TXG_ERR_NOMEM;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return TXG_ERR_NODEVICE;
+    return TXG_ERR_CUDA;
+}
+
+const char *last_error_text() { return g_err.c_str(); }
+
+static int fail(int code, const std::string &msg)
+{
+    g_err = msg;
+    return code;
+}
+
+static constexpr int NSLOT = 3;
+static constexpr long PREFETCH = 1 << 14; /* candidates copied back without waiting */
+static constexpr int NCLASS = 5;
+
+struct Slot {
+    txg_cand *dcand = nullptr; /* device [cap] */
+    int *dcount = nullptr;     /* device [2]: count, error code */
+    txg_cand *hcand = nullptr; /* pinned [PREFETCH] */
+    int *hcount = nullptr;     /* pinned [2] */
+    cudaEvent_t done = nullptr;
+    cudaEvent_t ev[NCLASS + 1] = {};
+    bool pending = false;
+    bool gated = false;
+    long counter = 0;
+};
+
+struct Result {
+    long counter = 0;
+    int gated = 0;
+    long count = 0;
+    std::vector<txg_cand> cands;
+};
+
+struct BeamRow {
+    float *xh[2] = {nullptr, nullptr};
+    int cur = 0;
+    float *ds = nullptr;
+    int32_t *ranges[8] = {nullptr};
+    float *z = nullptr, *b = nullptr, *s = nullptr;
+    double *sst = nullptr;
+    void *ring = nullptr;
+    float *tim = nullptr;
+    float *mxS = nullptr;
+    int32_t *mxwn = nullptr;
+    Slot slot[NSLOT];
+    long nblocks = 0;      /* blocks pushed */
+    long pushed = 0;       /* counter as of the last pushed block */
+    /* state of the most recently harvested block */
+    long counter = 0;
+    int gated = 0;
+    std::vector<txg_cand> last;
+    long last_count = 0;
+    bool overflow = false;
+    int dev_error = 0;
+    std::deque<Result> fifo;  /* harvested blocks not yet popped */
+};
+
+static constexpr size_t FIFO_MAX = 256;
+
+struct RowDev {
+    int32_t *sub_start = nullptr, *d1 = nullptr, *d2 = nullptr, *vwn = nullptr, *zap = nullptr;
+};
+
+} // namespace txg
+
+using namespace txg;
+
+struct txg_handle {
+    txg_plan plan;
+    std::vector<double> freqs;
+    std::vector<txg_row> rows;
+    std::vector<RowPlan> rp;
+    std::vector<RowDev> rd;
+    std::vector<std::vector<BeamRow>> br; /* [beam][row] */
+    cudaStream_t st = nullptr;
+    uint8_t *raw[2] = {nullptr, nullptr};
+    uint8_t *stage[2] = {nullptr, nullptr}; /* pinned staging for pageable host input */
+    cudaEvent_t raw_free[2] = {nullptr, nullptr};
+    int raw_cur = 0;
+    long cap = 0;
+    int prec = 0, flags = 0;
+    double class_ms[NCLASS] = {0};
+    long class_n[NCLASS] = {0};
+    std::vector<void *> allocs;
+};
+
+namespace {
+
+const char *status_text(int s)
+{
+    switch (s) {
+    case TXG_OK: return "ok";
+    case TXG_ERR_ARG: return "invalid argument";
+    case TXG_ERR_NOMEM: return "out of memory";
+    case TXG_ERR_CUDA: return "CUDA error";
+    case TXG_ERR_OVERFLOW: return "candidate buffer overflow";
+    case TXG_ERR_TIMEOUT: return "device wait timed out";
+    case TXG_ERR_STATE: return "invalid state";
+    case TXG_ERR_NODEVICE: return "no usable CUDA device";
+    case TXG_ERR_UNSUPPORTED: return "unsupported option";
+    default: return "unknown status";
+    }
+}
+
+template <typename T> int dalloc(txg_handle *h, T **p, size_t count)
+{
+    void *q = nullptr;
+    size_t bytes = count * sizeof(T);
+    if (bytes == 0) bytes = 16;
+    TXG_CUDA_TRY(cudaMalloc(&q, bytes));
+    h->allocs.push_back(q);
+    TXG_CUDA_TRY(cudaMemsetAsync(q, 0, bytes, h->st));
+    *p = (T *)q;
+    return TXG_OK;
+}
+
+template <typename T> int upload(txg_handle *h, T **p, const std::vector<T> &v)
+{
+    int rc = dalloc(h, p, v.size());
+    if (rc) return rc;
+    if (!v.empty())
+        TXG_CUDA_TRY(cudaMemcpyAsync(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, h->st));
+    return TXG_OK;
+}
+
+size_t ring_elem(int prec) { return prec == TXG_PREC_FP32 ? 4 : 2; }
+
+void free_all(txg_handle *h)
+{
+    if (h->st) cudaStreamSynchronize(h->st);
+    for (auto &beam : h->br)
+        for (auto &b : beam)
+            for (auto &sl : b.slot) {
+                if (sl.hcand) cudaFreeHost(sl.hcand);
+                if (sl.hcount) cudaFreeHost(sl.hcount);
+                if (sl.done) cudaEventDestroy(sl.done);
+                for (auto &e : sl.ev)
+                    if (e) cudaEventDestroy(e);
+            }
+    for (void *p : h->allocs) cudaFree(p);
+    h->allocs.clear();
+    for (int i = 0; i < 2; i++) {
+        if (h->stage[i]) cudaFreeHost(h->stage[i]);
+        if (h->raw_free[i]) cudaEventDestroy(h->raw_free[i]);
+    }
+    if (h->st) cudaStreamDestroy(h->st);
+    h->st = nullptr;
+}
+
+/* Collect one slot: wait for its block, sort its candidates into Cluster::run order and
+ * make them the row's last block. */
+int harvest_slot(txg_handle *h, BeamRow &b, Slot &sl)
+{
+    if (!sl.pending) return TXG_OK;
+    TXG_CUDA_TRY(cudaEventSynchronize(sl.done));
+    sl.pending = false;
+    if (h->flags & TXG_FLAG_TIMING) {
+        for (int c = 0; c < NCLASS; c++) {
+            if ((c == 3 || c == 4) && !sl.gated) continue;
+            float ms = 0.f;
+            TXG_CUDA_TRY(cudaEventElapsedTime(&ms, sl.ev[c], sl.ev[c + 1]));
+            h->class_ms[c] += ms;
+            h->class_n[c] += 1;
+        }
+    }
+    b.counter = sl.counter;
+    b.gated = sl.gated;
+    b.last.clear();
+    b.last_count = 0;
+    if (sl.hcount[1] != 0) {
+        b.dev_error = sl.hcount[1];
+        return fail(TXG_ERR_TIMEOUT, "a bounded device wait gave up (kernel code " +
+                                         std::to_string(sl.hcount[1]) + ")");
+    }
+    if (!sl.gated) return TXG_OK;
+    const long cnt = sl.hcount[0];
+    b.last_count = cnt;
+    const long keep = std::min(cnt, h->cap);
+    b.last.resize(keep);
+    const long pre = std::min(keep, PREFETCH);
+    if (pre > 0) memcpy(b.last.data(), sl.hcand, pre * sizeof(txg_cand));
+    if (keep > pre)
+        TXG_CUDA_TRY(cudaMemcpy(b.last.data() + pre, sl.dcand + pre, (keep - pre) * sizeof(txg_cand),
+                                cudaMemcpyDeviceToHost));
+    std::sort(b.last.begin(), b.last.end(), [](const txg_cand &x, const txg_cand &y) {
+        return x.idm != y.idm ? x.idm < y.idm : x.isamp < y.isamp;
+    });
+    int rc = TXG_OK;
+    if (cnt > h->cap) {
+        b.overflow = true;
+        rc = fail(TXG_ERR_OVERFLOW, "candidate buffer overflow: " + std::to_string(cnt) +
+                                        " points above threshold, capacity " + std::to_string(h->cap));
+    }
+    return rc;
+}
+
+void enqueue(BeamRow &b)
+{
+    if (b.fifo.size() >= FIFO_MAX) b.fifo.pop_front();
+    Result r;
+    r.counter = b.counter;
+    r.gated = b.gated;
+    r.count = b.last_count;
+    r.cands = b.last;
+    b.fifo.push_back(std::move(r));
+}
+
+int harvest(txg_handle *h, BeamRow &b, Slot &sl)
+{
+    if (!sl.pending) return TXG_OK;
+    int rc = harvest_slot(h, b, sl);
+    if (rc == TXG_OK || rc == TXG_ERR_OVERFLOW) enqueue(b);
+    return rc;
+}
+
+long pmod(long a, long m)
+{
+    long r = a % m;
+    return r < 0 ? r + m : r;
+}
+
+/* Queue every ddplan row of one block whose raw samples are at `raw` on the device. */
+int run_block(txg_handle *h, int beam, const uint8_t *raw)
+{
+    const long n0 = h->plan.ndump;
+    const int Craw = h->plan.nchans;
+    const bool timing = h->flags & TXG_FLAG_TIMING;
+    int status = TXG_OK;
+    for (size_t r = 0; r < h->rp.size(); r++) {
+        const RowPlan &P = h->rp[r];
+        RowDev &D = h->rd[r];
+        BeamRow &b = h->br[beam][r];
+        Slot &sl = b.slot[b.nblocks % NSLOT];
+        int rc = harvest(h, b, sl);
+        if (rc && rc != TXG_ERR_OVERFLOW) return rc;
+        if (rc) status = rc;
+        if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[0], h->st));
+
+        /* history: the last H columns of the previous block go in front of this one */
+        float *xprev = b.xh[b.cur ^ 1], *xcur = b.xh[b.cur];
+        if (P.H > 0)
+            TXG_CUDA_TRY(cudaMemcpy2DAsync(xcur, P.ldh * sizeof(float), xprev + P.N,
+                                           P.ldh * sizeof(float), P.H * sizeof(float), P.C,
+                                           cudaMemcpyDeviceToDevice, h->st));
+        float *x = xcur + P.H;
+        launch_unpack(raw, Craw, n0, P.cfg.td, P.cfg.fd, x, P.ldh, P.C, P.N, h->st);
+        if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[1], h->st));
+
+        launch_equalize(x, P.ldh, P.C, P.N, h->st);
+        if (P.bl_nw > 0) {
+            launch_colmean(x, P.ldh, P.C, P.N, b.z, h->st);
+            launch_smooth(b.z, P.N, P.bl_nw, b.b, h->st);
+            launch_sub_series(x, P.ldh, P.C, P.N, b.b, h->st);
+        }
+        if (!P.zap_chan.empty())
+            launch_zero_rows(x, P.ldh, D.zap, (int)P.zap_chan.size(), P.N, h->st);
+        for (int q = 0; q < P.cfg.nrfi; q++) {
+            if (P.cfg.rfi_kind[q] == TXG_RFI_KADANEF)
+                launch_kadane(x, P.ldh, P.C, P.N, P.cfg.rfi_td[q], P.cfg.rfi_fd[q], P.kad_thr,
+                              P.kad_wnlimit[q], b.ds, b.ranges[q], h->st);
+            else if (P.cfg.rfi_kind[q] == TXG_RFI_ZDOT)
+                launch_zdot(x, P.ldh, P.C, P.N, b.s, b.sst, h->st);
+        }
+        if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[2], h->st));
+
+        /* stage 1: new subband samples t in [counter-N-maxd1, counter-maxd1) */
+        const long counter = b.pushed + P.N;
+        const long tbase = counter - P.N - P.maxd1;
+        TXG_CUDA_TRY(cudaMemsetAsync(sl.dcount, 0, 2 * sizeof(int), h->st));
+        launch_stage1(xcur, P.ldh, P.H - P.maxd1, P.C, P.N, P.nsub, P.ng, D.sub_start, D.d1,
+                      P.maxd1, P.maxch, b.ring, P.R, pmod(tbase, P.R), h->prec, sl.dcount + 1,
+                      h->st);
+        TXG_CUDA_TRY(cudaGetLastError());
+        if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[3], h->st));
+
+        const bool gated = counter >= P.offset - P.noverlap + P.N;
+        if (gated) {
+            const long t0 = counter - P.N - P.offset;
+            launch_stage2(b.ring, P.R, P.nsub, P.G, P.cfg.ndm, P.nout, D.d2, P.s2_span,
+                          pmod(t0, P.R), h->prec, b.tim, P.nout, sl.dcount + 1, h->st);
+            TXG_CUDA_TRY(cudaGetLastError());
+            if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[4], h->st));
+            rc = launch_boxcar(b.tim, P.nout, P.cfg.ndm, P.nout, D.vwn, (int)P.vwn.size(),
+                               P.cfg.iqr, (h->flags & TXG_FLAG_AVX2_TAIL) ? 1 : 0, P.cfg.thre,
+                               sl.dcand, sl.dcount, h->cap, b.mxS, b.mxwn, sl.dcount + 1, h->st);
+            if (rc) return rc;
+            TXG_CUDA_TRY(cudaGetLastError());
+            if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[5], h->st));
+            TXG_CUDA_TRY(cudaMemcpyAsync(sl.hcand, sl.dcand, std::min(PREFETCH, h->cap) * sizeof(txg_cand),
+                                         cudaMemcpyDeviceToHost, h->st));
+        } else if (timing) {
+            TXG_CUDA_TRY(cudaEventRecord(sl.ev[4], h->st));
+            TXG_CUDA_TRY(cudaEventRecord(sl.ev[5], h->st));
+        }
+        TXG_CUDA_TRY(cudaMemcpyAsync(sl.hcount, sl.dcount, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+        TXG_CUDA_TRY(cudaEventRecord(sl.done, h->st));
+        sl.pending = true;
+        sl.gated = gated;
+        sl.counter = counter;
+        b.pushed = counter;
+        b.nblocks++;
+        b.cur ^= 1;
+    }
+    return status;
+}
+
+/* Device-layout decisions on top of plan_row: stage-2 window span, ring length, buffer
+ * pitch, and the limits of the kernels. */
+int finish_plan(RowPlan &P, int r)
+{
+    P.s2_span = stage2_span(P.d2.data(), P.nsub, P.G, P.cfg.ndm);
+    const long need = stage2_window(P.s2_span) + 64;
+    if (P.R < need) P.R = (need + 31) / 32 * 32;
+    P.maxch = 0;
+    for (int s = 0; s < P.nsub; s++) P.maxch = std::max(P.maxch, P.sub_start[s + 1] - P.sub_start[s]);
+    /* the stage-1 tile copy may read up to one tile past the block */
+    P.ldh = ((P.H + P.N + 256 + 16) + 31) / 32 * 32;
+    if ((size_t)P.nout > boxcar_max_samples())
+        return fail(TXG_ERR_UNSUPPORTED, "row " + std::to_string(r) +
+                                             ": ndump+noverlap exceeds the boxcar row limit of " +
+                                             std::to_string(boxcar_max_samples()) + " samples");
+    if (P.vwn.size() > 256) return fail(TXG_ERR_UNSUPPORTED, "more than 256 boxcar widths");
+    return TXG_OK;
+}
+
+void fill_info(const RowPlan &P, txg_row_info *out)
+{
+    memset(out, 0, sizeof(*out));
+    out->nchans = P.C;
+    out->nsub = P.nsub;
+    out->dm_group = P.G;
+    out->ngroup = P.ng;
+    out->nwidths = (int32_t)P.vwn.size();
+    out->maxwn = P.maxwn;
+    out->ndm = P.cfg.ndm;
+    out->ndump = P.N;
+    out->noverlap = P.noverlap;
+    out->offset = P.offset;
+    out->nsamples = P.nout;
+    out->maxd1 = P.maxd1;
+    out->maxd2 = P.maxd2;
+    out->tsamp = P.tsamp;
+    out->dms = P.cfg.dms;
+    out->ddm = P.cfg.ddm;
+    out->fmin = P.fmin;
+    out->fmax = P.fmax;
+}
+
+void copy_tables(const RowPlan &P, int32_t *d1, int32_t *d2, int32_t *sub_start, int32_t *vwn)
+{
+    if (d1) memcpy(d1, P.d1.data(), P.d1.size() * sizeof(int32_t));
+    if (d2) memcpy(d2, P.d2.data(), P.d2.size() * sizeof(int32_t));
+    if (sub_start) memcpy(sub_start, P.sub_start.data(), P.sub_start.size() * sizeof(int32_t));
+    if (vwn) memcpy(vwn, P.vwn.data(), P.vwn.size() * sizeof(int32_t));
+}
+
+int check_beam_row(txg_handle *h, int beam, int row)
+{
+    if (!h) return fail(TXG_ERR_ARG, "null handle");
+    if (beam < 0 || beam >= (int)h->br.size() || row < 0 || row >= (int)h->rp.size())
+        return fail(TXG_ERR_ARG, "beam or row out of range");
+    return TXG_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int32_t txg_version(void) { return TXG_ABI_VERSION; }
+
+const char *txg_strerror(int32_t status)
+{
+    static thread_local std::string s;
+    s = status_text(status);
+    if (status != TXG_OK && !g_err.empty()) s += ": " + g_err;
+    return s.c_str();
+}
+
+int txg_width_ladder(float minw, float maxw, float snrloss, double tsamp, int32_t *vwn, int32_t cap)
+{
+    if (!vwn || cap <= 0) return 0;
+    return width_ladder(minw, maxw, snrloss, tsamp, vwn, cap);
+}
+
+int txg_create(const txg_plan *plan, txg_handle **out)
+{
+    if (!plan || !out) return fail(TXG_ERR_ARG, "null plan or output");
+    *out = nullptr;
+    if (plan->nchans < 1 || plan->ndump < 1 || plan->nrows < 1 || plan->nbeams < 1 ||
+        !plan->frequencies || !plan->rows || plan->tsamp <= 0.)
+        return fail(TXG_ERR_ARG, "plan needs nchans, ndump, nrows, nbeams >= 1, tsamp > 0");
+    if (plan->precision < TXG_PREC_FP32 || plan->precision > TXG_PREC_FP16)
+        return fail(TXG_ERR_ARG, "unknown precision");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1)
+        return fail(TXG_ERR_NODEVICE, "no CUDA device");
+    txg_handle *h = new txg_handle();
+    h->plan = *plan;
+    h->freqs.assign(plan->frequencies, plan->frequencies + plan->nchans);
+    h->rows.assign(plan->rows, plan->rows + plan->nrows);
+    h->plan.frequencies = h->freqs.data();
+    h->plan.rows = h->rows.data();
+    h->prec = plan->precision;
+    h->flags = plan->flags;
+    h->cap = plan->cand_capacity > 0 ? plan->cand_capacity : (1L << 20);
+    int rc = TXG_OK;
+    h->rp.resize(plan->nrows);
+    for (int r = 0; r < plan->nrows && !rc; r++) {
+        std::string err;
+        rc = plan_row(h->rows[r], plan->nchans, h->freqs.data(), plan->tsamp, plan->ndump, h->rp[r], err);
+        if (rc) {
+            fail(rc, "row " + std::to_string(r) + ": " + err);
+            break;
+        }
+        rc = finish_plan(h->rp[r], r);
+    }
+    if (rc) {
+        delete h;
+        return rc;
+    }
+    if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) {
+        delete h;
+        return fail(TXG_ERR_CUDA, "cudaStreamCreate failed");
+    }
+    auto bail = [&](int code) {
+        free_all(h);
+        delete h;
+        return code;
+    };
+    const size_t raw_bytes = (size_t)plan->ndump * plan->nchans;
+    for (int i = 0; i < 2; i++) {
+        if ((rc = dalloc(h, &h->raw[i], raw_bytes))) return bail(rc);
+        if (cudaHostAlloc((void **)&h->stage[i], raw_bytes, cudaHostAllocDefault) != cudaSuccess)
+            return bail(fail(TXG_ERR_NOMEM, "pinned staging allocation failed"));
+        if (cudaEventCreateWithFlags(&h->raw_free[i], cudaEventDisableTiming) != cudaSuccess)
+            return bail(fail(TXG_ERR_CUDA, "event creation failed"));
+    }
+    h->rd.resize(plan->nrows);
+    for (int r = 0; r < plan->nrows; r++) {
+        RowPlan &P = h->rp[r];
+        RowDev &D = h->rd[r];
+        if ((rc = upload(h, &D.sub_start, P.sub_start)) || (rc = upload(h, &D.d1, P.d1)) ||
+            (rc = upload(h, &D.d2, P.d2)) || (rc = upload(h, &D.vwn, P.vwn)) ||
+            (rc = upload(h, &D.zap, P.zap_chan)))
+            return bail(rc);
+    }
+    h->br.resize(plan->nbeams);
+    for (int beam = 0; beam < plan->nbeams; beam++) {
+        h->br[beam].resize(plan->nrows);
+        for (int r = 0; r < plan->nrows; r++) {
+            RowPlan &P = h->rp[r];
+            BeamRow &b = h->br[beam][r];
+            for (int i = 0; i < 2; i++)
+                if ((rc = dalloc(h, &b.xh[i], (size_t)P.C * P.ldh))) return bail(rc);
+            long kmax = 1;
+            for (int q = 0; q < P.cfg.nrfi; q++)
+                if (P.cfg.rfi_kind[q] == TXG_RFI_KADANEF) {
+                    long nds = P.N / P.cfg.rfi_td[q], cds = P.C / P.cfg.rfi_fd[q];
+                    kmax = std::max(kmax, nds * cds);
+                    if ((rc = dalloc(h, &b.ranges[q], (size_t)4 * (cds + 1)))) return bail(rc);
+                }
+            if ((rc = dalloc(h, &b.ds, (size_t)kmax)) || (rc = dalloc(h, &b.z, (size_t)P.N)) ||
+                (rc = dalloc(h, &b.b, (size_t)P.N)) || (rc = dalloc(h, &b.s, (size_t)P.N)) ||
+                (rc = dalloc(h, &b.sst, (size_t)2)))
+                return bail(rc);
+            unsigned char *ring = nullptr;
+            if ((rc = dalloc(h, &ring, (size_t)P.ng * P.nsub * P.R * ring_elem(h->prec)))) return bail(rc);
+            b.ring = ring;
+            if ((rc = dalloc(h, &b.tim, (size_t)P.cfg.ndm * P.nout))) return bail(rc);
+            if (h->flags & TXG_FLAG_DENSE) {
+                if ((rc = dalloc(h, &b.mxS, (size_t)P.cfg.ndm * P.nout)) ||
+                    (rc = dalloc(h, &b.mxwn, (size_t)P.cfg.ndm * P.nout)))
+                    return bail(rc);
+            }
+            for (auto &sl : b.slot) {
+                if ((rc = dalloc(h, &sl.dcand, (size_t)h->cap)) || (rc = dalloc(h, &sl.dcount, (size_t)2)))
+                    return bail(rc);
+                if (cudaHostAlloc((void **)&sl.hcand, sizeof(txg_cand) * std::min(PREFETCH, h->cap),
+                                  cudaHostAllocDefault) != cudaSuccess ||
+                    cudaHostAlloc((void **)&sl.hcount, 2 * sizeof(int), cudaHostAllocDefault) != cudaSuccess)
+                    return bail(fail(TXG_ERR_NOMEM, "pinned candidate buffer allocation failed"));
+                sl.hcount[0] = sl.hcount[1] = 0;
+                if (cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) != cudaSuccess)
+                    return bail(fail(TXG_ERR_CUDA, "event creation failed"));
+                if (h->flags & TXG_FLAG_TIMING)
+                    for (auto &e : sl.ev)
+                        if (cudaEventCreate(&e) != cudaSuccess)
+                            return bail(fail(TXG_ERR_CUDA, "event creation failed"));
+            }
+        }
+    }
+    if (cudaStreamSynchronize(h->st) != cudaSuccess) return bail(fail(TXG_ERR_CUDA, "initialisation failed"));
+    *out = h;
+    return TXG_OK;
+}
+
+void txg_destroy(txg_handle *h)
+{
+    if (!h) return;
+    free_all(h);
+    delete h;
+}
+
+int txg_push_block_device(txg_handle *h, int32_t beam, const uint8_t *dev, int64_t nsamp)
+{
+    if (!h || !dev) return fail(TXG_ERR_ARG, "null handle or buffer");
+    if (beam < 0 || beam >= (int)h->br.size()) return fail(TXG_ERR_ARG, "beam out of range");
+    if (nsamp != h->plan.ndump) return fail(TXG_ERR_ARG, "nsamp must equal the plan's ndump");
+    return run_block(h, beam, dev);
+}
+
+int txg_push_block(txg_handle *h, int32_t beam, const uint8_t *host, int64_t nsamp)
+{
+    if (!h || !host) return fail(TXG_ERR_ARG, "null handle or buffer");
+    if (beam < 0 || beam >= (int)h->br.size()) return fail(TXG_ERR_ARG, "beam out of range");
+    if (nsamp != h->plan.ndump) return fail(TXG_ERR_ARG, "nsamp must equal the plan's ndump");
+    const size_t bytes = (size_t)nsamp * h->plan.nchans;
+    const int i = h->raw_cur;
+    h->raw_cur ^= 1;
+    /* the device buffer (and staging) of two blocks ago must be consumed */
+    TXG_CUDA_TRY(cudaEventSynchronize(h->raw_free[i]));
+    cudaPointerAttributes attr;
+    const bool pinned = cudaPointerGetAttributes(&attr, host) == cudaSuccess &&
+                        (attr.type == cudaMemoryTypeHost || attr.type == cudaMemoryTypeManaged);
+    const uint8_t *src = host;
+    if (!pinned) {
+        memcpy(h->stage[i], host, bytes);
+        src = h->stage[i];
+    }
+    TXG_CUDA_TRY(cudaMemcpyAsync(h->raw[i], src, bytes, cudaMemcpyHostToDevice, h->st));
+    int rc = run_block(h, beam, h->raw[i]);
+    TXG_CUDA_TRY(cudaEventRecord(h->raw_free[i], h->st));
+    return rc;
+}
+
+int txg_sync(txg_handle *h)
+{
+    if (!h) return fail(TXG_ERR_ARG, "null handle");
+    TXG_CUDA_TRY(cudaStreamSynchronize(h->st));
+    int status = TXG_OK;
+    for (auto &beam : h->br)
+        for (auto &b : beam) {
+            /* harvest in push order so `last` ends as the newest block */
+            for (long k = b.nblocks - NSLOT; k < b.nblocks; k++) {
+                if (k < 0) continue;
+                int rc = harvest(h, b, b.slot[k % NSLOT]);
+                if (rc && (status == TXG_OK || status == TXG_ERR_OVERFLOW)) status = rc;
+            }
+        }
+    return status;
+}
+
+int txg_get_row_info(txg_handle *h, int32_t beam, int32_t row, txg_row_info *out)
+{
+    int rc = check_beam_row(h, beam, row);
+    if (rc) return rc;
+    if (!out) return fail(TXG_ERR_ARG, "null output");
+    const BeamRow &b = h->br[beam][row];
+    fill_info(h->rp[row], out);
+    out->counter = b.counter;
+    out->gated = b.gated;
+    return TXG_OK;
+}
+
+int txg_get_candidates(txg_handle *h, int32_t beam, int32_t row, txg_cand *out, int64_t cap, int64_t *n)
+{
+    int rc = check_beam_row(h, beam, row);
+    if (rc) return rc;
+    const BeamRow &b = h->br[beam][row];
+    if (n) *n = b.last_count;
+    if (out && cap > 0) {
+        long m = std::min<long>(cap, (long)b.last.size());
+        if (m > 0) memcpy(out, b.last.data(), m * sizeof(txg_cand));
+    }
+    return b.last_count > h->cap ? TXG_ERR_OVERFLOW : TXG_OK;
+}
+
+int txg_pop_result(txg_handle *h, int32_t beam, int32_t row, int64_t *counter, int32_t *gated,
+                   txg_cand *out, int64_t cap, int64_t *n)
+{
+    int rc = check_beam_row(h, beam, row);
+    if (rc) return rc;
+    BeamRow &b = h->br[beam][row];
+    if (b.fifo.empty()) return fail(TXG_ERR_STATE, "no block result waiting");
+    Result &r = b.fifo.front();
+    if (counter) *counter = r.counter;
+    if (gated) *gated = r.gated;
+    if (n) *n = r.count;
+    if (out && cap > 0) {
+        long m = std::min<long>(cap, (long)r.cands.size());
+        if (m > 0) memcpy(out, r.cands.data(), m * sizeof(txg_cand));
+    }
+    const bool over = r.count > h->cap;
+    b.fifo.pop_front();
+    return over ? TXG_ERR_OVERFLOW : TXG_OK;
+}
+
+int txg_get_dense(txg_handle *h, int32_t beam, int32_t row, float *mxS, int32_t *mxwn)
+{
+    int rc = check_beam_row(h, beam, row);
+    if (rc) return rc;
+    if (!(h->flags & TXG_FLAG_DENSE)) return fail(TXG_ERR_STATE, "plan was created without TXG_FLAG_DENSE");
+    const RowPlan &P = h->rp[row];
+    const BeamRow &b = h->br[beam][row];
+    TXG_CUDA_TRY(cudaStreamSynchronize(h->st));
+    size_t cnt = (size_t)P.cfg.ndm * P.nout;
+    if (mxS) TXG_CUDA_TRY(cudaMemcpy(mxS, b.mxS, cnt * sizeof(float), cudaMemcpyDeviceToHost));
+    if (mxwn) TXG_CUDA_TRY(cudaMemcpy(mxwn, b.mxwn, cnt * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    return TXG_OK;
+}
+
+int txg_get_timdata(txg_handle *h, int32_t beam, int32_t row, int64_t idm0, int64_t count, float *out)
+{
+    int rc = check_beam_row(h, beam, row);
+    if (rc) return rc;
+    const RowPlan &P = h->rp[row];
+    if (!out || idm0 < 0 || count < 0 || idm0 + count > P.cfg.ndm) return fail(TXG_ERR_ARG, "DM range");
+    TXG_CUDA_TRY(cudaStreamSynchronize(h->st));
+    TXG_CUDA_TRY(cudaMemcpy(out, h->br[beam][row].tim + idm0 * P.nout, count * P.nout * sizeof(float),
+                            cudaMemcpyDeviceToHost));
+    return TXG_OK;
+}
+
+int txg_get_block(txg_handle *h, int32_t beam, int32_t row, float *out)
+{
+    int rc = check_beam_row(h, beam, row);
+    if (rc) return rc;
+    if (!out) return fail(TXG_ERR_ARG, "null output");
+    const RowPlan &P = h->rp[row];
+    const BeamRow &b = h->br[beam][row];
+    if (b.nblocks == 0) return fail(TXG_ERR_STATE, "no block pushed");
+    TXG_CUDA_TRY(cudaStreamSynchronize(h->st));
+    const float *x = b.xh[b.cur ^ 1] + P.H; /* buffer of the newest block */
+    TXG_CUDA_TRY(cudaMemcpy2D(out, P.N * sizeof(float), x, P.ldh * sizeof(float), P.N * sizeof(float), P.C,
+                              cudaMemcpyDeviceToHost));
+    return TXG_OK;
+}
+
+int txg_get_zap_ranges(txg_handle *h, int32_t beam, int32_t row, int32_t irfi, int32_t *out, int64_t cap)
+{
+    int rc = check_beam_row(h, beam, row);
+    if (rc) return rc;
+    const RowPlan &P = h->rp[row];
+    if (irfi < 0 || irfi >= P.cfg.nrfi || P.cfg.rfi_kind[irfi] != TXG_RFI_KADANEF)
+        return fail(TXG_ERR_ARG, "rfilist entry is not a kadaneF");
+    const long rows = P.C / P.cfg.rfi_fd[irfi];
+    if (!out || cap < 4 * rows) return fail(TXG_ERR_ARG, "output too small");
+    TXG_CUDA_TRY(cudaStreamSynchronize(h->st));
+    TXG_CUDA_TRY(cudaMemcpy(out, h->br[beam][row].ranges[irfi], 4 * rows * sizeof(int32_t),
+                            cudaMemcpyDeviceToHost));
+    return TXG_OK;
+}
+
+int txg_get_tables(txg_handle *h, int32_t row, int32_t *d1, int32_t *d2, int32_t *sub_start, int32_t *vwn)
+{
+    if (!h || row < 0 || row >= (int)h->rp.size()) return fail(TXG_ERR_ARG, "row out of range");
+    copy_tables(h->rp[row], d1, d2, sub_start, vwn);
+    return TXG_OK;
+}
+
+int txg_describe_row(const txg_plan *plan, int32_t row, txg_row_info *info, int32_t *d1, int32_t *d2,
+                     int32_t *sub_start, int32_t *vwn)
+{
+    if (!plan || !plan->rows || !plan->frequencies || row < 0 || row >= plan->nrows)
+        return fail(TXG_ERR_ARG, "bad plan or row");
+    RowPlan P;
+    std::string err;
+    int rc = plan_row(plan->rows[row], plan->nchans, plan->frequencies, plan->tsamp, plan->ndump, P, err);
+    if (rc) return fail(rc, err);
+    if ((rc = finish_plan(P, row))) return rc;
+    if (info) fill_info(P, info);
+    copy_tables(P, d1, d2, sub_start, vwn);
+    return TXG_OK;
+}
+
+int txg_get_timing(txg_handle *h, double *ms, int64_t *launches, int32_t n)
+{
+    if (!h) return fail(TXG_ERR_ARG, "null handle");
+    for (int c = 0; c < NCLASS && c < n; c++) {
+        if (ms) ms[c] = h->class_ms[c];
+        if (launches) launches[c] = h->class_n[c];
+        h->class_ms[c] = 0.;
+        h->class_n[c] = 0;
+    }
+    return NCLASS;
+}
+
+int txg_get_stream(txg_handle *h, void **stream)
+{
+    if (!h || !stream) return fail(TXG_ERR_ARG, "null argument");
+    *stream = (void *)h->st;
+    return TXG_OK;
+}
+
+int txg_boxcar(const float *tim, int64_t ndm, int64_t nsamples, const int32_t *vwn, int32_t nw,
+               int32_t iqr, int32_t flags, float thre, float *mxS, int32_t *mxwn, txg_cand *cands,
+               int64_t cap, int64_t *ncand)
+{
+    if (!tim || !vwn || ndm < 1 || nsamples < 1 || nw < 1 || nw > 256)
+        return fail(TXG_ERR_ARG, "need tim, vwn, ndm >= 1, nsamples >= 1, 1 <= nw <= 256");
+    if ((size_t)nsamples > boxcar_max_samples())
+        return fail(TXG_ERR_UNSUPPORTED, "nsamples exceeds the boxcar row limit");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return fail(TXG_ERR_NODEVICE, "no CUDA device");
+    cudaStream_t st;
+    TXG_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    float *dtim = nullptr, *dS = nullptr;
+    int32_t *dwn = nullptr, *dvwn = nullptr;
+    txg_cand *dc = nullptr;
+    int *dcount = nullptr;
+    const size_t cnt = (size_t)ndm * nsamples;
+    const long ccap = cands ? (cap > 0 ? cap : 0) : 0;
+    int rc = TXG_OK;
+    auto cleanup = [&]() {
+        cudaStreamSynchronize(st);
+        cudaFree(dtim);
+        cudaFree(dS);
+        cudaFree(dwn);
+        cudaFree(dvwn);
+        cudaFree(dc);
+        cudaFree(dcount);
+        cudaStreamDestroy(st);
+    };
+    do {
+        cudaError_t e;
+        if ((e = cudaMalloc(&dtim, cnt * sizeof(float))) != cudaSuccess ||
+            (e = cudaMalloc(&dvwn, nw * sizeof(int32_t))) != cudaSuccess ||
+            (e = cudaMalloc(&dcount, 2 * sizeof(int))) != cudaSuccess ||
+            (e = cudaMalloc(&dc, (ccap > 0 ? ccap : 1) * sizeof(txg_cand))) != cudaSuccess ||
+            (mxS && (e = cudaMalloc(&dS, cnt * sizeof(float))) != cudaSuccess) ||
+            (mxS && (e = cudaMalloc(&dwn, cnt * sizeof(int32_t))) != cudaSuccess)) {
+            rc = set_cuda_error(e, "cudaMalloc", __FILE__, __LINE__);
+            break;
+        }
+        if ((e = cudaMemcpyAsync(dtim, tim, cnt * sizeof(float), cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(dvwn, vwn, nw * sizeof(int32_t), cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+            (e = cudaMemsetAsync(dcount, 0, 2 * sizeof(int), st)) != cudaSuccess) {
+            rc = set_cuda_error(e, "copy-in", __FILE__, __LINE__);
+            break;
+        }
+        rc = launch_boxcar(dtim, nsamples, ndm, nsamples, dvwn, nw, iqr, (flags & TXG_FLAG_AVX2_TAIL) ? 1 : 0,
+                           thre, dc, dcount, ccap, dS, dwn, dcount + 1, st);
+        if (rc) break;
+        if ((e = cudaGetLastError()) != cudaSuccess) {
+            rc = set_cuda_error(e, "boxcar launch", __FILE__, __LINE__);
+            break;
+        }
+        int hc[2] = {0, 0};
+        if ((e = cudaMemcpyAsync(hc, dcount, 2 * sizeof(int), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+            (e = cudaStreamSynchronize(st)) != cudaSuccess) {
+            rc = set_cuda_error(e, "boxcar", __FILE__, __LINE__);
+            break;
+        }
+        if (mxS) {
+            if ((e = cudaMemcpy(mxS, dS, cnt * sizeof(float), cudaMemcpyDeviceToHost)) != cudaSuccess ||
+                (mxwn && (e = cudaMemcpy(mxwn, dwn, cnt * sizeof(int32_t), cudaMemcpyDeviceToHost)) != cudaSuccess)) {
+                rc = set_cuda_error(e, "copy-out", __FILE__, __LINE__);
+                break;
+            }
+        }
+        if (ncand) *ncand = hc[0];
+        if (cands && ccap > 0) {
+            long keep = std::min<long>(hc[0], ccap);
+            if (keep > 0 &&
+                (e = cudaMemcpy(cands, dc, keep * sizeof(txg_cand), cudaMemcpyDeviceToHost)) != cudaSuccess) {
+                rc = set_cuda_error(e, "copy-out", __FILE__, __LINE__);
+                break;
+            }
+            std::sort(cands, cands + keep, [](const txg_cand &x, const txg_cand &y) {
+                return x.idm != y.idm ? x.idm < y.idm : x.isamp < y.isamp;
+            });
+            if (hc[0] > ccap) rc = fail(TXG_ERR_OVERFLOW, "candidate buffer overflow");
+        }
+    } while (0);
+    cleanup();
+    return rc;
+}
+
+int txg_cluster(const txg_cand *cands, int64_t n, double dms, double ddm, double fmax, double fmin,
+                double tsamp, double radius_smearing, int32_t maxncand, int32_t minpts, int32_t drop,
+                int32_t maxwn, txg_cand *out, int64_t cap, int64_t *nout)
+{
+    if ((n > 0 && !cands) || n < 0 || tsamp <= 0.) return fail(TXG_ERR_ARG, "bad arguments");
+    long m = cluster_run(cands, n, dms, ddm, fmax, fmin, tsamp, radius_smearing, maxncand, minpts, drop,
+                         maxwn, out, out ? cap : 0);
+    if (nout) *nout = m;
+    return (out && m > cap) ? fail(TXG_ERR_OVERFLOW, "output too small") : TXG_OK;
+}
+
+} /* extern "C" */

@@ -1,0 +1,257 @@
+/*
+ * txg_boxcar.cu -- boxcar matched filter over dedispersed series, the Boxcar::match /
+ * Boxcar::run step (src/singlepulse/boxcar.cpp:158-296), fused with the S/N threshold and
+ * candidate compaction that feed Cluster::run (cluster.cpp:89-112).
+ *
+ * One CTA per DM row.  The row is staged in shared memory, its mean/variance reduced
+ * (FP32 runs combined in FP64), then the running sum of (x - mean) is formed in place by a
+ * block scan (per-thread FP32 chunks, FP64 chunk offsets) and every sample i keeps the
+ * largest S = (c[i+wh] - c[i-wl]) * sqrt(1/(wn*var)) over the width ladder, later widths
+ * winning ties (S >= best, best starting at 0) as in boxcar.cpp:253-262.  Rows with
+ * var <= 0 yield zeros (boxcar.cpp:242).  The IQR statistics (boxcar.cpp:215-227) come from
+ * an exact radix selection of the three order statistics.  Points with S > thre are appended
+ * to the candidate list with a warp-aggregated atomic; dense mxS/mxwn are optional.
+ */
+#include <cfloat>
+
+#include "txg_internal.h"
+
+namespace txg {
+
+namespace {
+
+constexpr int BX_THREADS = 512;
+constexpr unsigned FULL = 0xffffffffu;
+constexpr size_t BX_SMEM_MAX = 200 * 1024; /* + ~10 KB static stays under 227 KB */
+
+__device__ __forceinline__ double block_sum_d(double v, double *red)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) v = __dadd_rn(v, __shfl_xor_sync(FULL, v, off));
+    __syncthreads();
+    if (lane == 0) red[w] = v;
+    __syncthreads();
+    double t = 0.;
+    if (threadIdx.x < 32) {
+        t = threadIdx.x < (BX_THREADS / 32) ? red[threadIdx.x] : 0.;
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1) t = __dadd_rn(t, __shfl_xor_sync(FULL, t, off));
+        if (threadIdx.x == 0) red[0] = t;
+    }
+    __syncthreads();
+    return red[0];
+}
+
+/* float -> unsigned key with the same ordering */
+__device__ __forceinline__ unsigned fkey(float f)
+{
+    unsigned u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float fkey_inv(unsigned k)
+{
+    unsigned u = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+    return __uint_as_float(u);
+}
+
+/* Exact k-th smallest (0-based) of row[0..n) by 4 rounds of 8-bit radix selection. */
+__device__ float select_kth(const float *row, long n, long k, unsigned *hist)
+{
+    unsigned prefix = 0, mask = 0;
+    long kk = k;
+    for (int shift = 24; shift >= 0; shift -= 8) {
+        for (int b = threadIdx.x; b < 256; b += BX_THREADS) hist[b] = 0;
+        __syncthreads();
+        for (long i = threadIdx.x; i < n; i += BX_THREADS) {
+            unsigned key = fkey(row[i]);
+            if ((key & mask) == prefix) atomicAdd(&hist[(key >> shift) & 255u], 1u);
+        }
+        __syncthreads();
+        __shared__ unsigned sel_bin;
+        __shared__ long sel_rem;
+        if (threadIdx.x == 0) {
+            long acc = 0;
+            unsigned b = 0;
+            for (; b < 256; b++) {
+                if (acc + (long)hist[b] > kk) break;
+                acc += hist[b];
+            }
+            sel_bin = b;
+            sel_rem = kk - acc;
+        }
+        __syncthreads();
+        prefix |= sel_bin << shift;
+        mask |= 255u << shift;
+        kk = sel_rem;
+        __syncthreads();
+    }
+    return fkey_inv(prefix);
+}
+
+__global__ void __launch_bounds__(BX_THREADS)
+k_boxcar(const float *__restrict__ tim, long ldt, long n, const int32_t *__restrict__ vwn,
+         int nw, int iqr, int avx2_tail, float thre, txg_cand *__restrict__ cand,
+         int *__restrict__ ncand, long cap, float *__restrict__ mxS, int32_t *__restrict__ mxwn)
+{
+    extern __shared__ __align__(16) float c[];
+    __shared__ double red[BX_THREADS / 32];
+    __shared__ double chunk_off[BX_THREADS];
+    __shared__ float temp_w[256];
+    __shared__ int wl_w[256], wh_w[256], hi_w[256];
+    __shared__ unsigned hist[256];
+    __shared__ float mean_sh, var_sh;
+    const long k = blockIdx.x;
+    const int tid = threadIdx.x;
+    const float *row = tim + k * ldt;
+
+    for (long i = tid; i < n; i += BX_THREADS) c[i] = row[i];
+    __syncthreads();
+
+    if (!iqr) {
+        double s1 = 0., s2 = 0.;
+        long i = tid;
+        while (i < n) {
+            float r1 = 0.f, r2 = 0.f;
+            for (int r = 0; r < 8 && i < n; r++, i += BX_THREADS) {
+                float v = c[i];
+                r1 = __fadd_rn(r1, v);
+                r2 = __fadd_rn(r2, __fmul_rn(v, v));
+            }
+            s1 = __dadd_rn(s1, (double)r1);
+            s2 = __dadd_rn(s2, (double)r2);
+        }
+        s1 = block_sum_d(s1, red);
+        s2 = block_sum_d(s2, red);
+        if (tid == 0) {
+            double m = __ddiv_rn(s1, (double)n);
+            double v = __dsub_rn(__ddiv_rn(s2, (double)n), __dmul_rn(m, m));
+            mean_sh = __double2float_rn(m);
+            var_sh = __double2float_rn(v);
+        }
+    } else {
+        float q1 = select_kth(c, n, n / 4, hist);
+        float q2 = select_kth(c, n, n / 2, hist);
+        float q3 = select_kth(c, n, n - 1 - n / 4, hist);
+        if (tid == 0) {
+            double d = __ddiv_rn((double)__fsub_rn(q3, q1), 1.349);
+            mean_sh = q2;
+            var_sh = __double2float_rn(__dmul_rn(d, d));
+        }
+    }
+    __syncthreads();
+    const float mean = mean_sh, var = var_sh;
+
+    /* running sum of (x - mean): thread t owns the contiguous chunk [t*L, (t+1)*L) */
+    const long L = (n + BX_THREADS - 1) / BX_THREADS;
+    const long a = (long)tid * L, b = a + L < n ? a + L : n;
+    float loc = 0.f;
+    for (long i = a; i < b; i++) loc = __fadd_rn(loc, __fsub_rn(c[i], mean));
+    chunk_off[tid] = (double)loc;
+    __syncthreads();
+    if (tid < 32) { /* exclusive scan of the chunk totals in FP64 by one warp */
+        const int per = BX_THREADS / 32;
+        double v[BX_THREADS / 32];
+        double run = 0.;
+#pragma unroll
+        for (int q = 0; q < per; q++) {
+            v[q] = chunk_off[tid * per + q];
+            run = __dadd_rn(run, v[q]);
+        }
+        double incl = run;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            double y = __shfl_up_sync(FULL, incl, off);
+            if (tid >= off) incl = __dadd_rn(incl, y);
+        }
+        /* exclusive prefix = the left neighbour's inclusive sum */
+        const double left = __shfl_up_sync(FULL, incl, 1);
+        double ex = tid == 0 ? 0. : left;
+#pragma unroll
+        for (int q = 0; q < per; q++) {
+            chunk_off[tid * per + q] = ex;
+            ex = __dadd_rn(ex, v[q]);
+        }
+    }
+    __syncthreads();
+    {
+        const double off = chunk_off[tid];
+        float run = 0.f;
+        for (long i = a; i < b; i++) {
+            run = __fadd_rn(run, __fsub_rn(c[i], mean));
+            c[i] = __double2float_rn(__dadd_rn(off, (double)run));
+        }
+    }
+    for (int w = tid; w < nw; w += BX_THREADS) {
+        const int wn = vwn[w];
+        wl_w[w] = wn / 2 + 1;
+        wh_w[w] = (wn - 1) / 2;
+        temp_w[w] = __double2float_rn(__dsqrt_rn(__ddiv_rn(1., (double)__fmul_rn((float)wn, var))));
+        long hi = n - wh_w[w];
+        if (avx2_tail) {
+            long len = n - wh_w[w] - wl_w[w];
+            long nv = len >= 0 ? len / 8 : 0; /* C division truncates toward zero */
+            hi = nv > 0 ? wl_w[w] + 8 * nv : wl_w[w];
+        }
+        hi_w[w] = (int)hi;
+    }
+    __syncthreads();
+
+    const bool active = var > 0.f;
+    const int lane = tid & 31;
+    for (long base = 0; base < n; base += BX_THREADS) {
+        const long i = base + tid;
+        float best = 0.f;
+        int bw = 0;
+        if (active && i < n) {
+            for (int w = 0; w < nw; w++) {
+                const int wl = wl_w[w], wh = wh_w[w];
+                if (i >= wl && i < hi_w[w]) {
+                    const float S = __fmul_rn(__fsub_rn(c[i + wh], c[i - wl]), temp_w[w]);
+                    if (S >= best) {
+                        best = S;
+                        bw = vwn[w];
+                    } else if (avx2_tail && !(S < best)) {
+                        best = 0.f;
+                        bw = 0;
+                    }
+                }
+            }
+        }
+        if (i < n && mxS) {
+            mxS[k * n + i] = best;
+            mxwn[k * n + i] = bw;
+        }
+        const bool hit = i < n && best > thre;
+        const unsigned m = __ballot_sync(FULL, hit);
+        if (m) {
+            int basei = 0;
+            if (lane == __ffs(m) - 1) basei = atomicAdd(ncand, __popc(m));
+            basei = __shfl_sync(FULL, basei, __ffs(m) - 1);
+            if (hit) {
+                long slot = basei + __popc(m & ((1u << lane) - 1u));
+                if (slot < cap) cand[slot] = txg_cand{(int32_t)k, (int32_t)i, bw, best};
+            }
+        }
+    }
+}
+
+} // namespace
+
+size_t boxcar_max_samples() { return (BX_SMEM_MAX) / sizeof(float); }
+
+int launch_boxcar(const float *tim, long ldt, long ndm, long n, const int32_t *vwn, int nw,
+                  int iqr, int avx2_tail, float thre, txg_cand *cand, int *ncand, long cap,
+                  float *mxS, int32_t *mxwn, int *err, cudaStream_t st)
+{
+    (void)err;
+    if (n <= 0 || ndm <= 0) return TXG_OK;
+    if ((size_t)n > boxcar_max_samples() || nw > 256) return TXG_ERR_UNSUPPORTED;
+    size_t smem = (size_t)n * sizeof(float);
+    cudaFuncSetAttribute(k_boxcar, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BX_SMEM_MAX);
+    k_boxcar<<<(unsigned)ndm, BX_THREADS, smem, st>>>(tim, ldt, n, vwn, nw, iqr, avx2_tail, thre,
+                                                      cand, ncand, cap, mxS, mxwn);
+    return TXG_OK;
+}
+
+} // namespace txg

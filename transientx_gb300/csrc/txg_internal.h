@@ -1,0 +1,99 @@
+/*
+ * txg_internal.h -- internal declarations shared by the host planner, the C ABI and the
+ * CUDA kernels of the GB300 single-pulse search.
+ */
+#ifndef TXG_INTERNAL_H
+#define TXG_INTERNAL_H
+
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/transientx_gb300.h"
+
+namespace txg {
+
+/* Host-side plan of one ddplan row (beam independent). */
+struct RowPlan {
+    txg_row cfg;
+    int C = 0;            /* channels after fd */
+    long N = 0;           /* block samples after td */
+    double tsamp = 0.;    /* sampling time after td */
+    std::vector<double> freqs;
+    double fmax = 0., fmin = 0.;
+    /* subband dedispersion geometry */
+    int nsub = 0, G = 0, ng = 0;
+    long maxd1 = 0, maxd2 = 0, noverlap = 0, offset = 0, nout = 0;
+    long R = 0;           /* ring modulus (>= offset + N, multiple of 32) */
+    long H = 0;           /* history columns kept in front of each block (>= maxd1) */
+    long s2_span = 0;     /* largest d2 spread inside one stage-2 DM chunk */
+    int maxch = 0;        /* channels in the widest subband */
+    long ldh = 0;         /* row stride of the channel buffer */
+    std::vector<int32_t> sub_start; /* nsub+1 */
+    std::vector<double> fref;       /* nsub */
+    std::vector<int32_t> d1;        /* [ng][C] */
+    std::vector<int32_t> d2;        /* [ndm][nsub] */
+    std::vector<int32_t> vwn;
+    int maxwn = 0;
+    long bl_nw = 0;       /* baseline window in samples, 0 = off */
+    std::vector<int32_t> zap_chan;
+    long kad_wnlimit[8] = {0};
+    float kad_thr = 0.f;
+};
+
+/* Deterministic planning helpers (txg_plan.cpp). */
+double dmdelay(double dm, double fh, double fl);
+int width_ladder(float minw, float maxw, float snrloss, double tsamp, int32_t *vwn, int cap);
+int plan_row(const txg_row &cfg, int nchans_raw, const double *freqs_raw, double tsamp_raw,
+             long ndump_raw, RowPlan &out, std::string &err);
+int auto_nsub(int C, const std::vector<double> &freqs, double tsamp, double ddm, long ndm);
+int auto_group(int C, int nsub, const std::vector<double> &freqs, double tsamp, double ddm,
+               long ndm);
+
+/* Host clustering (txg_cluster.cpp). */
+long cluster_run(const txg_cand *c, long n, double dms, double ddm, double fmax, double fmin,
+                 double tsamp, double radius, int maxncand, int minpts, int drop, int maxwn,
+                 txg_cand *out, long cap);
+
+/* ---- kernel launchers (txg_pre.cu, txg_dedisp.cu, txg_boxcar.cu) -------------------- */
+void launch_unpack(const uint8_t *raw, int C_raw, long n0, int td, int fd, float *x, long ldx,
+                   int C, long N, cudaStream_t st);
+void launch_equalize(float *x, long ldx, int C, long N, cudaStream_t st);
+void launch_colmean(const float *x, long ldx, int C, long N, float *out, cudaStream_t st);
+void launch_smooth(const float *z, long N, long nw, float *b, cudaStream_t st);
+void launch_sub_series(float *x, long ldx, int C, long N, const float *b, cudaStream_t st);
+void launch_zero_rows(float *x, long ldx, const int32_t *rows, int nrows, long N,
+                      cudaStream_t st);
+void launch_kadane(float *x, long ldx, int C, long N, int tdk, int fdk, float thr,
+                   long wnlimit, float *ds, int32_t *ranges, cudaStream_t st);
+void launch_zdot(float *x, long ldx, int C, long N, float *s, double *sstats,
+                 cudaStream_t st);
+void launch_stage1(const float *xh, long ldh, long col0, int C, long N, int nsub, int ng,
+                   const int32_t *sub_start, const int32_t *d1, long maxd1, int maxch,
+                   void *ring, long R, long tbase_mod, int prec, int *err, cudaStream_t st);
+long stage2_span(const int32_t *d2h, int nsub, int G, long ndm);
+long stage2_window(long span);
+void launch_stage2(const void *ring, long R, int nsub, int G, long ndm, long nout,
+                   const int32_t *d2, long span, long t0_mod, int prec, float *tim, long ldt,
+                   int *err, cudaStream_t st);
+int launch_boxcar(const float *tim, long ldt, long ndm, long n, const int32_t *vwn, int nw,
+                  int iqr, int avx2_tail, float thre, txg_cand *cand, int *ncand, long cap,
+                  float *mxS, int32_t *mxwn, int *err, cudaStream_t st);
+size_t boxcar_max_samples();
+
+} // namespace txg
+
+#define TXG_CUDA_TRY(expr)                                                                  \
+    do {                                                                                    \
+        cudaError_t e_ = (expr);                                                            \
+        if (e_ != cudaSuccess) return txg::set_cuda_error(e_, #expr, __FILE__, __LINE__);   \
+    } while (0)
+
+namespace txg {
+int set_cuda_error(cudaError_t e, const char *expr, const char *file, int line);
+const char *last_error_text();
+} // namespace txg
+
+#endif
