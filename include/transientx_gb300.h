@@ -80,6 +80,8 @@ typedef struct {
     int32_t precision;         /* txg_precision */
     int32_t flags;             /* txg_flags */
     int64_t cand_capacity;     /* candidates kept per (beam,row,block); 0 = default */
+    float zapthre;             /* skewness/kurtosis channel zap of each raw block, IQR units
+                                * (PreprocessLite, dedisperse_fil.cpp:264-276,329); <= 0 off */
 } txg_plan;
 
 /* One point above threshold, in the order Cluster::run scans mxS (cluster.cpp:91-112). */
@@ -148,6 +150,10 @@ int txg_get_timdata(txg_handle *h, int32_t beam, int32_t row, int64_t idm0, int6
 int txg_get_block(txg_handle *h, int32_t beam, int32_t row, float *out);
 int txg_get_zap_ranges(txg_handle *h, int32_t beam, int32_t row, int32_t irfi, int32_t *out,
                        int64_t cap);
+
+/* Channels zapped by the skewness/kurtosis filter in the last block of a beam: mask[c] = 1
+ * (nchans raw channels). */
+int txg_get_mask(txg_handle *h, int32_t beam, uint8_t *mask);
 
 /* Integer tables of a row: within-subband delays d1 [ngroup][nchans], subband delays
  * d2 [ndm][nsub], first channel of each subband [nsub+1], width ladder [nwidths]. */

@@ -58,7 +58,7 @@ class Row(C.Structure):
         ("widthlimit", C.c_double), ("dms", C.c_double), ("ddm", C.c_double),
         ("ndm", C.c_long), ("overlap", C.c_double), ("nsub", C.c_int), ("group", C.c_int),
         ("minw", C.c_float), ("maxw", C.c_float), ("snrloss", C.c_float), ("iqr", C.c_int),
-        ("avx2_tail", C.c_int), ("thre", C.c_float),
+        ("avx2_tail", C.c_int), ("thre", C.c_float), ("zapthre", C.c_float),
     ]
 
 
@@ -88,6 +88,7 @@ def make_row(**kw) -> Row:
     r.iqr = int(kw.get("iqr", False))
     r.avx2_tail = int(kw.get("avx2_tail", False))
     r.thre = kw.get("thre", 7.0)
+    r.zapthre = kw.get("zapthre", -1.0)
     return r
 
 
@@ -110,10 +111,16 @@ def lib() -> C.CDLL:
     L.txo_kadane.argtypes = [f32p, C.c_long, C.POINTER(C.c_long), C.POINTER(C.c_long)]
     L.txo_red32.restype = C.c_double
     L.txo_red32.argtypes = [f32p, C.c_void_p, C.c_long, C.c_int]
-    L.txo_unpack_downsample.argtypes = [u8p, C.c_long, C.c_int, C.c_int, C.c_int, f32p, C.c_long]
+    L.txo_unpack_downsample.argtypes = [u8p, C.c_long, C.c_int, C.c_int, C.c_int, f32p, C.c_long,
+                                        C.c_void_p]
+    L.txo_sk_moments.argtypes = [u8p, C.c_long, C.c_int, f64p, f64p]
+    L.txo_skzap.restype = C.c_int
+    L.txo_skzap.argtypes = [u8p, C.c_long, C.c_int, C.c_float, u8p]
+    L.txo_sp_mask.restype = C.POINTER(C.c_uint8)
+    L.txo_sp_mask.argtypes = [C.c_void_p]
     L.txo_downsample_freqs.argtypes = [f64p, C.c_int, C.c_int, f64p]
-    L.txo_equalize.argtypes = [f32p, C.c_int, C.c_long, C.c_long]
-    L.txo_baseline.argtypes = [f32p, C.c_int, C.c_long, C.c_long, C.c_long]
+    L.txo_equalize.argtypes = [f32p, C.c_int, C.c_long, C.c_long, C.c_void_p]
+    L.txo_baseline.argtypes = [f32p, C.c_int, C.c_long, C.c_long, C.c_long, C.c_void_p]
     L.txo_zap_channels.argtypes = [f32p, C.c_int, C.c_long, C.c_long, f64p, f64p, C.c_int]
     L.txo_kadaneF.restype = C.c_int
     L.txo_kadaneF.argtypes = [f32p, C.c_int, C.c_long, C.c_long, C.c_int, C.c_int, C.c_float,
@@ -192,12 +199,29 @@ def red32(x, y=None, mode=0):
     return lib().txo_red32(x, yp, len(x), mode)
 
 
-def unpack_downsample(raw, td=1, fd=1):
+def unpack_downsample(raw, td=1, fd=1, mask=None):
     raw = np.ascontiguousarray(raw, np.uint8)
     n0, nchan = raw.shape
     x = np.zeros((nchan // fd, n0 // td), np.float32)
-    lib().txo_unpack_downsample(raw, n0, nchan, td, fd, x, x.shape[1])
+    m = None if mask is None else np.ascontiguousarray(mask, np.uint8)
+    lib().txo_unpack_downsample(raw, n0, nchan, td, fd, x, x.shape[1],
+                                None if m is None else m.ctypes.data)
     return x
+
+
+def sk_moments(raw):
+    raw = np.ascontiguousarray(raw, np.uint8)
+    sk = np.zeros(raw.shape[1], np.float64)
+    ku = np.zeros(raw.shape[1], np.float64)
+    lib().txo_sk_moments(raw, raw.shape[0], raw.shape[1], sk, ku)
+    return sk, ku
+
+
+def skzap(raw, thr):
+    raw = np.ascontiguousarray(raw, np.uint8)
+    mask = np.zeros(raw.shape[1], np.uint8)
+    lib().txo_skzap(raw, raw.shape[0], raw.shape[1], thr, mask)
+    return mask
 
 
 def downsample_freqs(f, fd):
@@ -209,13 +233,15 @@ def downsample_freqs(f, fd):
 
 def equalize(x):
     x = np.array(x, np.float32, order="C", copy=True)
-    lib().txo_equalize(x, x.shape[0], x.shape[1], x.shape[1])
-    return x
+    live = np.zeros(x.shape[0], np.uint8)
+    lib().txo_equalize(x, x.shape[0], x.shape[1], x.shape[1], live.ctypes.data)
+    return x, live
 
 
-def baseline(x, nw):
+def baseline(x, nw, live=None):
     x = np.array(x, np.float32, order="C", copy=True)
-    lib().txo_baseline(x, x.shape[0], x.shape[1], x.shape[1], nw)
+    live = np.ones(x.shape[0], np.uint8) if live is None else np.ascontiguousarray(live, np.uint8)
+    lib().txo_baseline(x, x.shape[0], x.shape[1], x.shape[1], nw, live.ctypes.data)
     return x
 
 
@@ -311,6 +337,7 @@ class SinglePulseRow:
         self.h = lib().txo_sp_create(C.byref(row), len(f), f, tsamp, ndump)
         if not self.h:
             raise ValueError("invalid row parameters")
+        self.nchan_raw = len(f)
 
     def run(self, raw) -> bool:
         raw = np.ascontiguousarray(raw, np.uint8)
@@ -331,6 +358,10 @@ class SinglePulseRow:
         p = lib().txo_sp_block(self.h, C.byref(ldx), C.byref(nch), C.byref(n))
         a = np.ctypeslib.as_array(p, shape=(nch.value, ldx.value))
         return a[:, : n.value].copy()
+
+    def mask(self):
+        p = lib().txo_sp_mask(self.h)
+        return np.ctypeslib.as_array(p, shape=(self.nchan_raw,)).copy()
 
     def zap_ranges(self, irfi):
         nrows = C.c_int()

@@ -110,10 +110,81 @@ double txo_red32(const float *x, const float *y, long n, int mode)
     return acc[0];
 }
 
+/* Skewness-kurtosis channel zap of the raw block (the PreprocessLite filter of
+ * dedisperse_fil.cpp:264-276,329, method of docs/pipeline/rfi_mitigation.rst "Skewness-Kurtosis
+ * filter"; outlier rule as Candidate::azap, candidate.cpp:622-652).  Per channel the central
+ * moments come from exact integer sums of (v-128)^p; skewness m3/m2^1.5 and excess kurtosis
+ * m4/m2^2-3 (0 for constant channels); a channel is zapped when either lies outside
+ * [Q1 - thr*R, Q3 + thr*R] with Q1 = sorted[n/4], Q3 = sorted[n-1-n/4], R = Q3-Q1.
+ * mask[c] = 1 marks a zapped channel.  thr <= 0 disables the filter. */
+static int cmp_double(const void *a, const void *b)
+{
+    double x = *(const double *)a, y = *(const double *)b;
+    return (x > y) - (x < y);
+}
+
+void txo_sk_moments(const uint8_t *raw, long n0, int nchan, double *skew, double *kurt)
+{
+#pragma omp parallel for num_threads(nthr())
+    for (int c = 0; c < nchan; c++) {
+        int64_t s1 = 0, s2 = 0, s3 = 0, s4 = 0;
+        for (long t = 0; t < n0; t++) {
+            int64_t v = (int64_t)raw[t * (long)nchan + c] - 128;
+            int64_t v2 = v * v;
+            s1 += v;
+            s2 += v2;
+            s3 += v2 * v;
+            s4 += v2 * v2;
+        }
+        const double n = (double)n0;
+        const double a = (double)s1 / n, b = (double)s2 / n, cc = (double)s3 / n, d = (double)s4 / n;
+        const double aa = a * a;
+        const double m2 = b - aa;
+        const double m3 = (cc - 3. * a * b) + 2. * aa * a;
+        const double m4 = ((d - 4. * a * cc) + 6. * aa * b) - 3. * aa * aa;
+        if (m2 > 0.) {
+            skew[c] = m3 / (m2 * sqrt(m2));
+            kurt[c] = m4 / (m2 * m2) - 3.;
+        } else {
+            skew[c] = 0.;
+            kurt[c] = 0.;
+        }
+    }
+}
+
+int txo_skzap(const uint8_t *raw, long n0, int nchan, float thr, uint8_t *mask)
+{
+    memset(mask, 0, nchan);
+    if (!(thr > 0.f) || nchan < 1 || n0 < 1) return 0;
+    double *sk = (double *)malloc(sizeof(double) * nchan), *ku = (double *)malloc(sizeof(double) * nchan);
+    double *srt = (double *)malloc(sizeof(double) * nchan);
+    txo_sk_moments(raw, n0, nchan, sk, ku);
+    double lo[2], hi[2];
+    for (int q = 0; q < 2; q++) {
+        memcpy(srt, q == 0 ? sk : ku, sizeof(double) * nchan);
+        qsort(srt, nchan, sizeof(double), cmp_double);
+        double q1 = srt[nchan / 4], q3 = srt[nchan - 1 - nchan / 4], R = q3 - q1;
+        lo[q] = q1 - (double)thr * R;
+        hi[q] = q3 + (double)thr * R;
+    }
+    int nz = 0;
+    for (int c = 0; c < nchan; c++) {
+        if (sk[c] < lo[0] || sk[c] > hi[0] || ku[c] < lo[1] || ku[c] > hi[1]) {
+            mask[c] = 1;
+            nz++;
+        }
+    }
+    free(sk);
+    free(ku);
+    free(srt);
+    return nz;
+}
+
 /* uint8 time-major raw block [n0][nchan] -> channel-major sums of td x fd neighbours
- * (src/singlepulse/candidate.cpp:395-407: k over fd outer, n over td inner). */
+ * (src/singlepulse/candidate.cpp:395-407: k over fd outer, n over td inner); channels with
+ * mask[c] != 0 contribute 0 (weight 0 as in candidate.cpp:603-618). */
 void txo_unpack_downsample(const uint8_t *raw, long n0, int nchan, int td, int fd, float *x,
-                           long ldx)
+                           long ldx, const uint8_t *mask)
 {
     int nc = nchan / fd;
     long nn = n0 / td;
@@ -121,9 +192,11 @@ void txo_unpack_downsample(const uint8_t *raw, long n0, int nchan, int td, int f
     for (int j = 0; j < nc; j++) {
         for (long i = 0; i < nn; i++) {
             float acc = 0.f;
-            for (int k = 0; k < fd; k++)
+            for (int k = 0; k < fd; k++) {
+                const long c = (long)j * fd + k;
                 for (int t = 0; t < td; t++)
-                    acc = acc + (float)raw[(i * td + t) * (long)nchan + (long)j * fd + k];
+                    acc = acc + (mask && mask[c] ? 0.f : (float)raw[(i * td + t) * (long)nchan + c]);
+            }
             x[(long)j * ldx + i] = acc;
         }
     }
@@ -144,7 +217,7 @@ void txo_downsample_freqs(const double *f, int nchan, int fd, double *out)
  * the integer-valued sum-downsample of uint8 data, so the sums are exact in int64; the
  * standard deviation falls back to 1 when the variance is not positive (as
  * candidate.cpp:850 does for zdot). */
-void txo_equalize(float *x, int nchan, long n, long ldx)
+void txo_equalize(float *x, int nchan, long n, long ldx, uint8_t *live)
 {
     if (n <= 0) return;
 #pragma omp parallel for num_threads(nthr())
@@ -161,23 +234,44 @@ void txo_equalize(float *x, int nchan, long n, long ldx)
         double sd = var > 0. ? sqrt(var) : 1.;
         float mf = (float)mean, inv = (float)(1. / sd);
         for (long i = 0; i < n; i++) r[i] = (r[i] - mf) * inv;
+        if (live) live[j] = var > 0. ? 1 : 0;
     }
 }
 
+/* Channel sum at sample i in the fixed order both implementations use: 8 consecutive
+ * channel blocks of ceil(nchan/8), each summed from 0.0f, block sums added in order. */
+static float colsum8(const float *x, int nchan, long ldx, long i)
+{
+    const int cb = (nchan + 7) / 8;
+    float t = 0.f;
+    for (int q = 0; q < 8; q++) {
+        float acc = 0.f;
+        const int j1 = (q + 1) * cb < nchan ? (q + 1) * cb : nchan;
+        for (int j = q * cb; j < j1; j++) acc = acc + x[(long)j * ldx + i];
+        t = t + acc;
+    }
+    return t;
+}
+
 /* Subtract the smoothed zero-DM series (docs/pipeline/preprocess.rst:26-29): z[i] is the
- * channel mean at sample i, b[i] the mean of z over [i-nw/2, i+nw/2] clipped to the block. */
-void txo_baseline(float *x, int nchan, long n, long ldx, long nw)
+ * mean over live channels at sample i, b[i] the mean of z over [i-nw/2, i+nw/2] clipped to
+ * the block; b is subtracted from live channels only.  A channel is live when its block had
+ * non-zero variance at Equalize (dead and zapped channels are exactly 0 there and stay 0). */
+void txo_baseline(float *x, int nchan, long n, long ldx, long nw, const uint8_t *live)
 {
     if (nw <= 0 || n <= 0) return;
     float *z = (float *)malloc(sizeof(float) * n);
     float *b = (float *)malloc(sizeof(float) * n);
     long h = nw / 2;
-#pragma omp parallel for num_threads(nthr())
-    for (long i = 0; i < n; i++) {
-        float acc = 0.f;
-        for (int j = 0; j < nchan; j++) acc = acc + x[(long)j * ldx + i];
-        z[i] = acc / (float)nchan;
+    int nlive = 0;
+    for (int j = 0; j < nchan; j++) nlive += live[j] ? 1 : 0;
+    if (nlive == 0) {
+        free(z);
+        free(b);
+        return;
     }
+#pragma omp parallel for num_threads(nthr())
+    for (long i = 0; i < n; i++) z[i] = colsum8(x, nchan, ldx, i) / (float)nlive;
 #pragma omp parallel for num_threads(nthr())
     for (long i = 0; i < n; i++) {
         long lo = i - h < 0 ? 0 : i - h;
@@ -188,7 +282,8 @@ void txo_baseline(float *x, int nchan, long n, long ldx, long nw)
     }
 #pragma omp parallel for num_threads(nthr())
     for (int j = 0; j < nchan; j++)
-        for (long i = 0; i < n; i++) x[(long)j * ldx + i] = x[(long)j * ldx + i] - b[i];
+        if (live[j])
+            for (long i = 0; i < n; i++) x[(long)j * ldx + i] = x[(long)j * ldx + i] - b[i];
     free(z);
     free(b);
 }
@@ -284,11 +379,7 @@ void txo_zdot(float *x, int nchan, long n, long ldx)
         for (long i = 0; i < n; i++) r[i] = (r[i] - mf) * inv;
     }
 #pragma omp parallel for num_threads(nthr())
-    for (long i = 0; i < n; i++) {
-        float acc = 0.f;
-        for (int j = 0; j < nchan; j++) acc = acc + x[(long)j * ldx + i];
-        s[i] = acc / (float)nchan;
-    }
+    for (long i = 0; i < n; i++) s[i] = colsum8(x, nchan, ldx, i) / (float)nchan;
     double se = txo_red32(s, 0, n, 0), ss = txo_red32(s, 0, n, 1);
     double tmp = se * se - ss * (double)n;
 #pragma omp parallel for num_threads(nthr())
@@ -740,6 +831,7 @@ const float *txo_dedisp_timdata(const txo_dedisp *dd) { return dd->tim; }
  * ------------------------------------------------------------------------------------- */
 struct txo_sp {
     txo_row row;
+    uint8_t *mask, *live;
     int nchan_raw, nchan;
     long ndump_raw, n;
     double tsamp;
@@ -770,6 +862,8 @@ txo_sp *txo_sp_create(const txo_row *row, int nchan, const double *freqs, double
     txo_downsample_freqs(freqs, nchan, row->fd, sp->freqs);
     sp->ldx = sp->n;
     sp->x = (float *)calloc((size_t)sp->nchan * sp->ldx, sizeof(float));
+    sp->mask = (uint8_t *)calloc(nchan, 1);
+    sp->live = (uint8_t *)calloc(sp->nchan, 1);
     for (int r = 0; r < row->nrfi && r < 8; r++)
         if (row->rfi_kind[r] == TXO_RFI_KADANEF)
             sp->ranges[r] = (int32_t *)calloc((size_t)4 * (sp->nchan / row->rfi_fd[r] + 1), 4);
@@ -791,6 +885,8 @@ void txo_sp_destroy(txo_sp *sp)
     if (!sp) return;
     free(sp->freqs);
     free(sp->x);
+    free(sp->mask);
+    free(sp->live);
     for (int r = 0; r < 8; r++) free(sp->ranges[r]);
     txo_dedisp_destroy(sp->dd);
     free(sp->mxS);
@@ -801,10 +897,12 @@ void txo_sp_destroy(txo_sp *sp)
 int txo_sp_run(txo_sp *sp, const uint8_t *raw)
 {
     const txo_row *row = &sp->row;
-    txo_unpack_downsample(raw, sp->ndump_raw, sp->nchan_raw, row->td, row->fd, sp->x, sp->ldx);
-    txo_equalize(sp->x, sp->nchan, sp->n, sp->ldx);
+    txo_skzap(raw, sp->ndump_raw, sp->nchan_raw, row->zapthre, sp->mask);
+    txo_unpack_downsample(raw, sp->ndump_raw, sp->nchan_raw, row->td, row->fd, sp->x, sp->ldx,
+                          sp->mask);
+    txo_equalize(sp->x, sp->nchan, sp->n, sp->ldx, sp->live);
     long nw = row->bswidth > 0.f ? (long)round((double)row->bswidth / sp->tsamp) : 0;
-    txo_baseline(sp->x, sp->nchan, sp->n, sp->ldx, nw);
+    txo_baseline(sp->x, sp->nchan, sp->n, sp->ldx, nw, sp->live);
     if (row->nzap > 0)
         txo_zap_channels(sp->x, sp->nchan, sp->n, sp->ldx, sp->freqs, &row->zap[0][0], row->nzap);
     for (int r = 0; r < row->nrfi && r < 8; r++) {
@@ -848,6 +946,7 @@ const int32_t *txo_sp_zap_ranges(const txo_sp *sp, int irfi, int *nrows)
 }
 
 const float *txo_sp_timdata(const txo_sp *sp) { return sp->dd->tim; }
+const uint8_t *txo_sp_mask(const txo_sp *sp) { return sp->mask; }
 const float *txo_sp_mxS(const txo_sp *sp) { return sp->mxS; }
 const int *txo_sp_mxwn(const txo_sp *sp) { return sp->mxwn; }
 void txo_sp_freqs(const txo_sp *sp, double *out)

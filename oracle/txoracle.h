@@ -7,6 +7,8 @@
  *
  * What is restated from where (paths relative to the TransientX source tree):
  *   - stage order of one ddplan row ........ src/singlepulse/singlepulse.cpp:287-341
+ *   - skewness/kurtosis channel zap ........ dedisperse_fil.cpp:264-276,329 (PreprocessLite),
+ *                                            outlier rule as candidate.cpp:622-652
  *   - boxcar width ladder .................. src/singlepulse/singlepulse.cpp:242-254
  *   - time/frequency sum-downsample ......... src/singlepulse/candidate.cpp:381-427
  *   - kadaneF zapping ...................... src/singlepulse/candidate.cpp:710-829,
@@ -38,11 +40,13 @@ float txo_kadane(const float *y, long n, long *start, long *end);
 double txo_red32(const float *x, const float *y, long n, int mode);
 
 /* ---- preprocessing of one block, channel-major x[j*ldx + i] --------------------------- */
+void txo_sk_moments(const uint8_t *raw, long n0, int nchan, double *skew, double *kurt);
+int txo_skzap(const uint8_t *raw, long n0, int nchan, float thr, uint8_t *mask);
 void txo_unpack_downsample(const uint8_t *raw, long n0, int nchan, int td, int fd,
-                           float *x, long ldx);
+                           float *x, long ldx, const uint8_t *mask);
 void txo_downsample_freqs(const double *f, int nchan, int fd, double *out);
-void txo_equalize(float *x, int nchan, long n, long ldx);
-void txo_baseline(float *x, int nchan, long n, long ldx, long nw);
+void txo_equalize(float *x, int nchan, long n, long ldx, uint8_t *live);
+void txo_baseline(float *x, int nchan, long n, long ldx, long nw, const uint8_t *live);
 void txo_zap_channels(float *x, int nchan, long n, long ldx, const double *freqs,
                       const double *zap, int nzap);
 int txo_kadaneF(float *x, int nchan, long n, long ldx, int tdk, int fdk, float thr,
@@ -106,6 +110,7 @@ typedef struct {
     float minw, maxw, snrloss;
     int iqr, avx2_tail;
     float thre;
+    float zapthre;
 } txo_row;
 
 typedef struct txo_sp txo_sp;
@@ -118,6 +123,7 @@ void txo_sp_dedisp_info(const txo_sp *sp, txo_dedisp_info *info);
 const float *txo_sp_block(const txo_sp *sp, long *ldx, int *nchan, long *n);
 const int32_t *txo_sp_zap_ranges(const txo_sp *sp, int irfi, int *nrows);
 const float *txo_sp_timdata(const txo_sp *sp);
+const uint8_t *txo_sp_mask(const txo_sp *sp);
 const float *txo_sp_mxS(const txo_sp *sp);
 const int *txo_sp_mxwn(const txo_sp *sp);
 void txo_sp_freqs(const txo_sp *sp, double *out);

@@ -29,7 +29,7 @@ def small_workload(seed=21, nsamples=4096 * 6):
     return fil, rows, 4096
 
 
-def oracle_rows(oracle, rows, fil, ndump, tx, avx2=False):
+def oracle_rows(oracle, rows, fil, ndump, tx, avx2=False, zapthre=4.0):
     out = []
     for r, sp in enumerate(rows):
         info = tx.describe_row(rows, r, fil.nchans, fil.tsamp, fil.freqs, ndump)[0]
@@ -37,25 +37,29 @@ def oracle_rows(oracle, rows, fil, ndump, tx, avx2=False):
                               threKadaneF=sp.threKadaneF, widthlimit=sp.widthlimit, dms=sp.dms,
                               ddm=sp.ddm, ndm=sp.ndm, overlap=sp.overlap, nsub=info.nsub,
                               group=info.dm_group, minw=sp.minw, maxw=sp.maxw,
-                              snrloss=sp.snrloss, iqr=sp.iqr, thre=sp.thre, avx2_tail=avx2)
+                              snrloss=sp.snrloss, iqr=sp.iqr, thre=sp.thre, avx2_tail=avx2,
+                              zapthre=zapthre)
         out.append(oracle.SinglePulseRow(row, fil.freqs, fil.tsamp, ndump))
     return out
 
 
-@pytest.mark.parametrize("avx2", [False, True])
-def test_pipeline_fp32_matches_oracle(tx, oracle, avx2):
+@pytest.mark.parametrize("avx2,zapthre", [(False, 4.0), (True, 4.0), (False, 0.0)])
+def test_pipeline_fp32_matches_oracle(tx, oracle, avx2, zapthre):
     fil, rows, ndump = small_workload()
     flags = tx.FLAG_DENSE | tx.FLAG_KEEP_SERIES | (tx.FLAG_AVX2_TAIL if avx2 else 0)
-    orows = oracle_rows(oracle, rows, fil, ndump, tx, avx2)
+    orows = oracle_rows(oracle, rows, fil, ndump, tx, avx2, zapthre)
     nblk = fil.nsamples // ndump
     ngated = 0
-    with tx.Search(rows, fil.nchans, fil.tsamp, fil.freqs, ndump, flags=flags) as s:
+    with tx.Search(rows, fil.nchans, fil.tsamp, fil.freqs, ndump, flags=flags,
+                   zapthre=zapthre) as s:
         for b in range(nblk):
             raw = fil.generate(b * ndump, ndump)
             s.push_block(raw)
             s.sync()
             for r, o in enumerate(orows):
                 gated = o.run(raw)
+                if zapthre > 0:
+                    np.testing.assert_array_equal(s.mask(), o.mask())
                 info = s.row_info(r)
                 assert bool(info.gated) == gated and info.counter == o.info().counter
                 np.testing.assert_array_equal(s.block(r), o.block(), err_msg=f"block {b} row {r}")
@@ -74,10 +78,23 @@ def test_pipeline_fp32_matches_oracle(tx, oracle, avx2):
     assert ngated >= 4
 
 
+def test_skzap_catches_sinusoids(tx, oracle):
+    fil, rows, ndump = small_workload()
+    sines = sorted(c for c, _, _, _ in fil.sines)
+    with tx.Search(rows[:1], fil.nchans, fil.tsamp, fil.freqs, ndump, zapthre=4.0) as s:
+        for b in range(2):
+            raw = fil.generate(b * ndump, ndump)
+            s.push_block(raw)
+            s.sync()
+            m = s.mask()
+            np.testing.assert_array_equal(m, oracle.skzap(raw, 4.0))
+            assert m[sines].all()
+
+
 def test_kadane_fires_on_rfi(tx, oracle):
     fil, rows, ndump = small_workload()
     with tx.Search(rows[:1], fil.nchans, fil.tsamp, fil.freqs, ndump,
-                   flags=tx.FLAG_KEEP_SERIES) as s:
+                   flags=tx.FLAG_KEEP_SERIES, zapthre=0.0) as s:
         s.push_block(fil.generate(0, ndump))
         s.sync()
         zr = s.zap_ranges(0)

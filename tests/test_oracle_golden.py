@@ -72,3 +72,23 @@ def test_kadane_definition(oracle):
     assert oracle.kadane([-3, -1, -2]) == (-1.0, 1, 1)          # all negative: best element
     assert oracle.kadane([2, -2, 2]) == (2.0, 0, 0)             # tie: earliest window kept
     assert oracle.kadane([0, 0, 5]) == (5.0, 0, 2)              # zero sum does not restart
+
+
+def test_skzap_moments_match_numpy(oracle):
+    """Channel skewness/kurtosis of the oracle against a float64 numpy evaluation."""
+    rng = np.random.default_rng(4)
+    raw = np.clip(np.round(rng.normal(128, 12, (3000, 64))), 0, 255).astype(np.uint8)
+    raw[:, 5] = 77                                               # constant channel
+    raw[:, 9] = (128 + 40 * np.sin(np.arange(3000) / 7.0)).astype(np.uint8)  # sinusoid
+    sk, ku = oracle.sk_moments(raw)
+    v = raw.astype(np.float64)
+    d = v - v.mean(0)
+    m2, m3, m4 = (d ** 2).mean(0), (d ** 3).mean(0), (d ** 4).mean(0)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        rsk = np.where(m2 > 0, m3 / m2 ** 1.5, 0.0)
+        rku = np.where(m2 > 0, m4 / m2 ** 2 - 3.0, 0.0)
+    np.testing.assert_allclose(sk, rsk, atol=1e-9)
+    np.testing.assert_allclose(ku, rku, atol=1e-9)
+    mask = oracle.skzap(raw, 4.0)
+    assert mask[9] == 1 and mask.sum() <= 3
+    assert not oracle.skzap(raw, 0.0).any()       # threshold <= 0 disables the filter

@@ -55,7 +55,7 @@ class txg_plan(C.Structure):
         ("nchans", C.c_int32), ("tsamp", C.c_double), ("frequencies", C.POINTER(C.c_double)),
         ("ndump", C.c_int64), ("nrows", C.c_int32), ("rows", C.POINTER(txg_row)),
         ("nbeams", C.c_int32), ("precision", C.c_int32), ("flags", C.c_int32),
-        ("cand_capacity", C.c_int64),
+        ("cand_capacity", C.c_int64), ("zapthre", C.c_float),
     ]
 
 
@@ -78,7 +78,7 @@ EXPORTS = [
     "txg_get_row_info", "txg_get_candidates", "txg_get_dense", "txg_get_timdata",
     "txg_get_block", "txg_get_zap_ranges", "txg_get_tables", "txg_width_ladder", "txg_boxcar",
     "txg_cluster", "txg_get_timing", "txg_get_stream", "txg_strerror", "txg_version",
-    "txg_describe_row", "txg_pop_result",
+    "txg_describe_row", "txg_pop_result", "txg_get_mask",
 ]
 
 _lib: Optional[C.CDLL] = None
@@ -119,6 +119,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
                               C.c_int32, vp, C.c_int64, C.POINTER(C.c_int64)]
     L.txg_get_timing.argtypes = [vp, vp, vp, C.c_int32]
     L.txg_get_stream.argtypes = [vp, C.POINTER(vp)]
+    L.txg_get_mask.argtypes = [vp, C.c_int32, vp]
     L.txg_pop_result.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(C.c_int64),
                                  C.POINTER(C.c_int32), vp, C.c_int64, C.POINTER(C.c_int64)]
     L.txg_describe_row.argtypes = [C.POINTER(txg_plan), C.c_int32, C.POINTER(txg_row_info), vp,
@@ -238,7 +239,8 @@ def width_ladder(minw: float, maxw: float, snrloss: float, tsamp: float) -> np.n
     return out[:n].copy()
 
 
-def _make_plan(rows, nchans, tsamp, freqs, ndump, nbeams, precision, flags, cand_capacity):
+def _make_plan(rows, nchans, tsamp, freqs, ndump, nbeams, precision, flags, cand_capacity,
+               zapthre=0.0):
     crows = (txg_row * len(rows))(*[r.to_c() for r in rows])
     plan = txg_plan()
     plan.nchans, plan.tsamp = nchans, tsamp
@@ -246,6 +248,7 @@ def _make_plan(rows, nchans, tsamp, freqs, ndump, nbeams, precision, flags, cand
     plan.ndump, plan.nrows, plan.rows = ndump, len(rows), crows
     plan.nbeams, plan.precision, plan.flags = nbeams, PRECISIONS[precision], flags
     plan.cand_capacity = cand_capacity
+    plan.zapthre = zapthre
     return plan, crows
 
 
@@ -274,7 +277,10 @@ class Search:
 
     def __init__(self, rows: Sequence[SinglePulse], nchans: int, tsamp: float,
                  frequencies: Sequence[float], ndump: int, nbeams: int = 1,
-                 precision: str = "fp32", flags: int = 0, cand_capacity: int = 0):
+                 precision: str = "fp32", flags: int = 0, cand_capacity: int = 0,
+                 zapthre: float = 4.0):
+        """zapthre: skewness/kurtosis channel-zap threshold in IQR units, the --zapthre of
+        transientx_fil (default 4, dedisperse_fil.cpp:56); <= 0 disables it."""
         L = load_library()
         self.rows = list(rows)
         self.nchans, self.tsamp, self.ndump, self.nbeams = nchans, tsamp, ndump, nbeams
@@ -282,7 +288,8 @@ class Search:
         if len(self._freqs) != nchans:
             raise ValueError("need one frequency per channel")
         plan, self._crows = _make_plan(self.rows, nchans, tsamp, self._freqs, ndump, nbeams,
-                                       precision, flags, cand_capacity)
+                                       precision, flags, cand_capacity, zapthre)
+        self.zapthre = zapthre
         self.cap = cand_capacity if cand_capacity > 0 else 1 << 20
         self.flags = flags
         h = vp()
@@ -374,6 +381,11 @@ class Search:
         i = self.row_info(row, beam)
         out = np.zeros((i.nchans, i.ndump), np.float32)
         _check(load_library().txg_get_block(self.h, beam, row, _ptr(out)), "block")
+        return out
+
+    def mask(self, beam: int = 0) -> np.ndarray:
+        out = np.zeros(self.nchans, np.uint8)
+        _check(load_library().txg_get_mask(self.h, beam, _ptr(out)), "mask")
         return out
 
     def zap_ranges(self, irfi: int, row: int = 0, beam: int = 0) -> np.ndarray:

@@ -71,6 +71,7 @@ struct BeamRow {
     int32_t *ranges[8] = {nullptr};
     float *z = nullptr, *b = nullptr, *s = nullptr;
     double *sst = nullptr;
+    uint8_t *live = nullptr;
     void *ring = nullptr;
     float *tim = nullptr;
     float *mxS = nullptr;
@@ -94,6 +95,13 @@ struct RowDev {
     int32_t *sub_start = nullptr, *d1 = nullptr, *d2 = nullptr, *vwn = nullptr, *zap = nullptr;
 };
 
+/* Per-beam scratch of the skewness/kurtosis channel zap. */
+struct BeamPrep {
+    unsigned long long *sums = nullptr; /* [4][nchans] */
+    double *stats = nullptr;            /* [2][nchans] */
+    uint8_t *mask = nullptr;            /* [nchans] */
+};
+
 } // namespace txg
 
 using namespace txg;
@@ -105,6 +113,7 @@ struct txg_handle {
     std::vector<RowPlan> rp;
     std::vector<RowDev> rd;
     std::vector<std::vector<BeamRow>> br; /* [beam][row] */
+    std::vector<BeamPrep> prep;           /* [beam] */
     cudaStream_t st = nullptr;
     uint8_t *raw[2] = {nullptr, nullptr};
     uint8_t *stage[2] = {nullptr, nullptr}; /* pinned staging for pageable host input */
@@ -259,6 +268,13 @@ int run_block(txg_handle *h, int beam, const uint8_t *raw)
     const int Craw = h->plan.nchans;
     const bool timing = h->flags & TXG_FLAG_TIMING;
     int status = TXG_OK;
+    const uint8_t *mask = nullptr;
+    if (h->plan.zapthre > 0.f) {
+        BeamPrep &bp = h->prep[beam];
+        launch_skzap(raw, Craw, n0, h->plan.zapthre, bp.sums, bp.stats, bp.mask, h->st);
+        TXG_CUDA_TRY(cudaGetLastError());
+        mask = bp.mask;
+    }
     for (size_t r = 0; r < h->rp.size(); r++) {
         const RowPlan &P = h->rp[r];
         RowDev &D = h->rd[r];
@@ -276,14 +292,14 @@ int run_block(txg_handle *h, int beam, const uint8_t *raw)
                                            P.ldh * sizeof(float), P.H * sizeof(float), P.C,
                                            cudaMemcpyDeviceToDevice, h->st));
         float *x = xcur + P.H;
-        launch_unpack(raw, Craw, n0, P.cfg.td, P.cfg.fd, x, P.ldh, P.C, P.N, h->st);
+        launch_unpack(raw, Craw, n0, P.cfg.td, P.cfg.fd, x, P.ldh, P.C, P.N, mask, h->st);
         if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[1], h->st));
 
-        launch_equalize(x, P.ldh, P.C, P.N, h->st);
+        launch_equalize(x, P.ldh, P.C, P.N, b.live, h->st);
         if (P.bl_nw > 0) {
-            launch_colmean(x, P.ldh, P.C, P.N, b.z, h->st);
+            launch_colmean(x, P.ldh, P.C, P.N, b.live, b.z, h->st);
             launch_smooth(b.z, P.N, P.bl_nw, b.b, h->st);
-            launch_sub_series(x, P.ldh, P.C, P.N, b.b, h->st);
+            launch_sub_series(x, P.ldh, P.C, P.N, b.b, b.live, h->st);
         }
         if (!P.zap_chan.empty())
             launch_zero_rows(x, P.ldh, D.zap, (int)P.zap_chan.size(), P.N, h->st);
@@ -433,6 +449,11 @@ int txg_create(const txg_plan *plan, txg_handle **out)
     h->rows.assign(plan->rows, plan->rows + plan->nrows);
     h->plan.frequencies = h->freqs.data();
     h->plan.rows = h->rows.data();
+    if (plan->zapthre > 0.f && (size_t)plan->nchans > skzap_max_channels()) {
+        delete h;
+        return fail(TXG_ERR_UNSUPPORTED, "the channel zap handles at most " +
+                                             std::to_string(skzap_max_channels()) + " channels");
+    }
     h->prec = plan->precision;
     h->flags = plan->flags;
     h->cap = plan->cand_capacity > 0 ? plan->cand_capacity : (1L << 20);
@@ -478,7 +499,13 @@ int txg_create(const txg_plan *plan, txg_handle **out)
             return bail(rc);
     }
     h->br.resize(plan->nbeams);
+    h->prep.resize(plan->nbeams);
     for (int beam = 0; beam < plan->nbeams; beam++) {
+        BeamPrep &bp = h->prep[beam];
+        if ((rc = dalloc(h, &bp.sums, (size_t)4 * plan->nchans)) ||
+            (rc = dalloc(h, &bp.stats, (size_t)2 * plan->nchans)) ||
+            (rc = dalloc(h, &bp.mask, (size_t)plan->nchans)))
+            return bail(rc);
         h->br[beam].resize(plan->nrows);
         for (int r = 0; r < plan->nrows; r++) {
             RowPlan &P = h->rp[r];
@@ -493,6 +520,7 @@ int txg_create(const txg_plan *plan, txg_handle **out)
                     if ((rc = dalloc(h, &b.ranges[q], (size_t)4 * (cds + 1)))) return bail(rc);
                 }
             if ((rc = dalloc(h, &b.ds, (size_t)kmax)) || (rc = dalloc(h, &b.z, (size_t)P.N)) ||
+                (rc = dalloc(h, &b.live, (size_t)P.C)) ||
                 (rc = dalloc(h, &b.b, (size_t)P.N)) || (rc = dalloc(h, &b.s, (size_t)P.N)) ||
                 (rc = dalloc(h, &b.sst, (size_t)2)))
                 return bail(rc);
@@ -681,6 +709,15 @@ int txg_get_zap_ranges(txg_handle *h, int32_t beam, int32_t row, int32_t irfi, i
     TXG_CUDA_TRY(cudaStreamSynchronize(h->st));
     TXG_CUDA_TRY(cudaMemcpy(out, h->br[beam][row].ranges[irfi], 4 * rows * sizeof(int32_t),
                             cudaMemcpyDeviceToHost));
+    return TXG_OK;
+}
+
+int txg_get_mask(txg_handle *h, int32_t beam, uint8_t *mask)
+{
+    if (!h || !mask) return fail(TXG_ERR_ARG, "null argument");
+    if (beam < 0 || beam >= (int)h->prep.size()) return fail(TXG_ERR_ARG, "beam out of range");
+    TXG_CUDA_TRY(cudaStreamSynchronize(h->st));
+    TXG_CUDA_TRY(cudaMemcpy(mask, h->prep[beam].mask, h->plan.nchans, cudaMemcpyDeviceToHost));
     return TXG_OK;
 }
 

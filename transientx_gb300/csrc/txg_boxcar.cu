@@ -21,6 +21,7 @@ namespace txg {
 namespace {
 
 constexpr int BX_THREADS = 512;
+constexpr int BX_U = 4; /* samples per thread per pass: width parameters loaded once for all */
 constexpr unsigned FULL = 0xffffffffu;
 constexpr size_t BX_SMEM_MAX = 200 * 1024; /* + ~10 KB static stays under 227 KB */
 
@@ -98,7 +99,7 @@ k_boxcar(const float *__restrict__ tim, long ldt, long n, const int32_t *__restr
     __shared__ double red[BX_THREADS / 32];
     __shared__ double chunk_off[BX_THREADS];
     __shared__ float temp_w[256];
-    __shared__ int wl_w[256], wh_w[256], hi_w[256];
+    __shared__ int4 wpar[256]; /* wl, wh, end of the visited range, wn */
     __shared__ unsigned hist[256];
     __shared__ float mean_sh, var_sh;
     const long k = blockIdx.x;
@@ -184,53 +185,65 @@ k_boxcar(const float *__restrict__ tim, long ldt, long n, const int32_t *__restr
     }
     for (int w = tid; w < nw; w += BX_THREADS) {
         const int wn = vwn[w];
-        wl_w[w] = wn / 2 + 1;
-        wh_w[w] = (wn - 1) / 2;
+        const int wl = wn / 2 + 1, wh = (wn - 1) / 2;
         temp_w[w] = __double2float_rn(__dsqrt_rn(__ddiv_rn(1., (double)__fmul_rn((float)wn, var))));
-        long hi = n - wh_w[w];
+        long hi = n - wh;
         if (avx2_tail) {
-            long len = n - wh_w[w] - wl_w[w];
+            long len = n - wh - wl;
             long nv = len >= 0 ? len / 8 : 0; /* C division truncates toward zero */
-            hi = nv > 0 ? wl_w[w] + 8 * nv : wl_w[w];
+            hi = nv > 0 ? wl + 8 * nv : wl;
         }
-        hi_w[w] = (int)hi;
+        wpar[w] = make_int4(wl, wh, (int)hi, wn);
     }
     __syncthreads();
 
     const bool active = var > 0.f;
     const int lane = tid & 31;
-    for (long base = 0; base < n; base += BX_THREADS) {
-        const long i = base + tid;
-        float best = 0.f;
-        int bw = 0;
-        if (active && i < n) {
+    for (long base = 0; base < n; base += (long)BX_THREADS * BX_U) {
+        float best[BX_U];
+        int bw[BX_U];
+#pragma unroll
+        for (int u = 0; u < BX_U; u++) {
+            best[u] = 0.f;
+            bw[u] = 0;
+        }
+        if (active) {
             for (int w = 0; w < nw; w++) {
-                const int wl = wl_w[w], wh = wh_w[w];
-                if (i >= wl && i < hi_w[w]) {
-                    const float S = __fmul_rn(__fsub_rn(c[i + wh], c[i - wl]), temp_w[w]);
-                    if (S >= best) {
-                        best = S;
-                        bw = vwn[w];
-                    } else if (avx2_tail && !(S < best)) {
-                        best = 0.f;
-                        bw = 0;
+                const int4 p = wpar[w];
+                const float tw = temp_w[w];
+#pragma unroll
+                for (int u = 0; u < BX_U; u++) {
+                    const long i = base + tid + (long)u * BX_THREADS;
+                    if (i >= p.x && i < p.z) {
+                        const float S = __fmul_rn(__fsub_rn(c[i + p.y], c[i - p.x]), tw);
+                        if (S >= best[u]) {
+                            best[u] = S;
+                            bw[u] = p.w;
+                        } else if (avx2_tail && !(S < best[u])) {
+                            best[u] = 0.f;
+                            bw[u] = 0;
+                        }
                     }
                 }
             }
         }
-        if (i < n && mxS) {
-            mxS[k * n + i] = best;
-            mxwn[k * n + i] = bw;
-        }
-        const bool hit = i < n && best > thre;
-        const unsigned m = __ballot_sync(FULL, hit);
-        if (m) {
-            int basei = 0;
-            if (lane == __ffs(m) - 1) basei = atomicAdd(ncand, __popc(m));
-            basei = __shfl_sync(FULL, basei, __ffs(m) - 1);
-            if (hit) {
-                long slot = basei + __popc(m & ((1u << lane) - 1u));
-                if (slot < cap) cand[slot] = txg_cand{(int32_t)k, (int32_t)i, bw, best};
+#pragma unroll
+        for (int u = 0; u < BX_U; u++) {
+            const long i = base + tid + (long)u * BX_THREADS;
+            if (i < n && mxS) {
+                mxS[k * n + i] = best[u];
+                mxwn[k * n + i] = bw[u];
+            }
+            const bool hit = i < n && best[u] > thre;
+            const unsigned m = __ballot_sync(FULL, hit);
+            if (m) {
+                int basei = 0;
+                if (lane == __ffs(m) - 1) basei = atomicAdd(ncand, __popc(m));
+                basei = __shfl_sync(FULL, basei, __ffs(m) - 1);
+                if (hit) {
+                    const long slot = basei + __popc(m & ((1u << lane) - 1u));
+                    if (slot < cap) cand[slot] = txg_cand{(int32_t)k, (int32_t)i, bw[u], best[u]};
+                }
             }
         }
     }

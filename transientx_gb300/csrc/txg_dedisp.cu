@@ -210,6 +210,7 @@ k_stage2(const T *__restrict__ ring, long R, int nsub, int G, long ndm, long nou
     T *win = reinterpret_cast<T *>(smraw);
     int32_t *doff = reinterpret_cast<int32_t *>(smraw + ((wtot_max * sizeof(T) + 15) / 16) * 16);
     int32_t *wbeg = doff + sc * S2_KPC;
+    int32_t *wts = wbeg + sc, *wal = wts + sc, *wlen = wal + sc, *wpos = wlen + sc;
     const int tid = threadIdx.x;
     const int nkc = (G + S2_KPC - 1) / S2_KPC;
     const int g = blockIdx.y / nkc, kc = blockIdx.y % nkc;
@@ -240,38 +241,50 @@ k_stage2(const T *__restrict__ ring, long R, int nsub, int G, long ndm, long nou
             int lo = d2[(size_t)k0 * nsub + s0 + ss];
             doff[e] = k < kn ? d2[(size_t)(k0 + k) * nsub + s0 + ss] - lo : 0;
         }
-        if (tid == 0) {
-            /* pass 1: total bytes, so the barrier expects them before any copy lands */
-            uint32_t total = 0;
-            for (int ss = 0; ss < sn; ss++) {
-                const int s = s0 + ss;
-                const long lo = d2[(size_t)k0 * nsub + s];
-                const long hi = d2[(size_t)(k0 + kn - 1) * nsub + s];
-                const long al = ((t0_mod + u0 + lo) % R) % EPC;
-                const long len = ((long)S2_TT + (hi - lo) + al + EPC - 1) / EPC * EPC;
-                total += (uint32_t)(len * sizeof(T));
+        /* window of each subband: ring start rounded down to 16 bytes, length, offset */
+        for (int ss = tid; ss < sn; ss += S2_THREADS) {
+            const int s = s0 + ss;
+            const long lo = d2[(size_t)k0 * nsub + s];
+            const long hi = d2[(size_t)(k0 + kn - 1) * nsub + s];
+            long tstart = (t0_mod + u0 + lo) % R;
+            const long al = tstart % EPC;
+            tstart -= al;
+            wts[ss] = (int32_t)tstart;
+            wal[ss] = (int32_t)al;
+            wlen[ss] = (int32_t)(((long)S2_TT + (hi - lo) + al + EPC - 1) / EPC * EPC);
+        }
+        __syncthreads();
+        if (tid < 32) { /* exclusive prefix of the lengths (one warp) */
+            int carry = 0;
+            for (int base = 0; base < sn; base += 32) {
+                const int ss = base + tid;
+                const int v = ss < sn ? wlen[ss] : 0;
+                int incl = v;
+#pragma unroll
+                for (int off = 1; off < 32; off <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, incl, off);
+                    if (tid >= off) incl += y;
+                }
+                if (ss < sn) wpos[ss] = carry + incl - v;
+                carry += __shfl_sync(0xffffffffu, incl, 31);
             }
+            if (tid == 0) {
+                fence_proxy_async();
+                mbar_expect_tx(&bar, (uint32_t)(carry * (int)sizeof(T)));
+            }
+        }
+        __syncthreads();
+        for (int ss = tid; ss < sn; ss += S2_THREADS) {
+            const T *row = ring + ((size_t)g * nsub + s0 + ss) * R;
+            const long pos = wpos[ss], len = wlen[ss], tstart = wts[ss];
+            wbeg[ss] = (int32_t)(pos + wal[ss]);
+            /* split at the ring end; R is a multiple of 32 elements and exceeds len, so both
+             * parts are whole 16-byte units inside the row */
+            const long first = min(len, R - tstart);
             fence_proxy_async();
-            mbar_expect_tx(&bar, total);
-            long pos = 0;
-            for (int ss = 0; ss < sn; ss++) {
-                const int s = s0 + ss;
-                const long lo = d2[(size_t)k0 * nsub + s];
-                const long hi = d2[(size_t)(k0 + kn - 1) * nsub + s];
-                long tstart = (t0_mod + u0 + lo) % R;
-                const long al = tstart % EPC;
-                tstart -= al;
-                const long len = ((long)S2_TT + (hi - lo) + al + EPC - 1) / EPC * EPC;
-                wbeg[ss] = (int32_t)(pos + al);
-                const T *row = ring + ((size_t)g * nsub + s) * R;
-                /* split at the ring end; R is a multiple of 32 elements and exceeds len, so
-                 * both parts are whole 16-byte units inside the row */
-                const long first = min(len, R - tstart);
-                bulk_g2s(win + pos, row + tstart, (uint32_t)(first * sizeof(T)), &bar);
-                if (first < len)
-                    bulk_g2s(win + pos + first, row, (uint32_t)((len - first) * sizeof(T)), &bar);
-                pos += len;
-            }
+            bulk_g2s(win + pos, row + tstart, (uint32_t)(first * sizeof(T)), &bar);
+            if (first < len)
+                bulk_g2s(win + pos + first, row, (uint32_t)((len - first) * sizeof(T)), &bar);
         }
         __syncthreads();
         bool ok = mbar_wait(&bar, phase);
@@ -313,7 +326,7 @@ k_stage2(const T *__restrict__ ring, long R, int nsub, int G, long ndm, long nou
 
 inline unsigned nblk(long n, int b) { return (unsigned)((n + b - 1) / b); }
 
-constexpr size_t SMEM_BUDGET = 200 * 1024;
+constexpr size_t SMEM_BUDGET = 100 * 1024; /* two CTAs per SM overlap copies and math */
 
 } // namespace
 
@@ -370,12 +383,12 @@ static void stage2_impl(const void *ring, long R, int nsub, int G, long ndm, lon
 {
     const long epc = 16 / (long)sizeof(T);
     const long wlen = ((long)S2_TT + span + 2 * epc) / epc * epc;
-    const size_t per = wlen * sizeof(T) + S2_KPC * sizeof(int32_t) + sizeof(int32_t);
+    const size_t per = wlen * sizeof(T) + S2_KPC * sizeof(int32_t) + 5 * sizeof(int32_t);
     int sc = (int)((SMEM_BUDGET - 64) / per);
     if (sc > nsub) sc = nsub;
     if (sc < 1) sc = 1;
     const long wtot = (long)sc * wlen;
-    const size_t smem = ((wtot * sizeof(T) + 15) / 16) * 16 + (size_t)sc * S2_KPC * 4 + (size_t)sc * 4;
+    const size_t smem = ((wtot * sizeof(T) + 15) / 16) * 16 + (size_t)sc * S2_KPC * 4 + (size_t)sc * 5 * 4;
     const int nkc = (G + S2_KPC - 1) / S2_KPC;
     const long ng = (ndm + G - 1) / G;
     dim3 grid(nblk(nout, S2_TT), (unsigned)(ng * nkc));

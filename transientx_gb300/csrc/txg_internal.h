@@ -58,12 +58,17 @@ long cluster_run(const txg_cand *c, long n, double dms, double ddm, double fmax,
                  txg_cand *out, long cap);
 
 /* ---- kernel launchers (txg_pre.cu, txg_dedisp.cu, txg_boxcar.cu) -------------------- */
+void launch_skzap(const uint8_t *raw, int C_raw, long n0, float thr, unsigned long long *sums,
+                  double *stats, uint8_t *mask, cudaStream_t st);
+size_t skzap_max_channels();
 void launch_unpack(const uint8_t *raw, int C_raw, long n0, int td, int fd, float *x, long ldx,
-                   int C, long N, cudaStream_t st);
-void launch_equalize(float *x, long ldx, int C, long N, cudaStream_t st);
-void launch_colmean(const float *x, long ldx, int C, long N, float *out, cudaStream_t st);
+                   int C, long N, const uint8_t *mask, cudaStream_t st);
+void launch_equalize(float *x, long ldx, int C, long N, uint8_t *live, cudaStream_t st);
+void launch_colmean(const float *x, long ldx, int C, long N, const uint8_t *live, float *out,
+                    cudaStream_t st);
 void launch_smooth(const float *z, long N, long nw, float *b, cudaStream_t st);
-void launch_sub_series(float *x, long ldx, int C, long N, const float *b, cudaStream_t st);
+void launch_sub_series(float *x, long ldx, int C, long N, const float *b, const uint8_t *live,
+                       cudaStream_t st);
 void launch_zero_rows(float *x, long ldx, const int32_t *rows, int nrows, long N,
                       cudaStream_t st);
 void launch_kadane(float *x, long ldx, int C, long N, int tdk, int fdk, float thr,

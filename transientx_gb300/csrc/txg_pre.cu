@@ -56,6 +56,111 @@ __device__ __forceinline__ double red32(const float *__restrict__ x, const float
     return warp_sum_d(acc);
 }
 
+/* ---- skewness/kurtosis channel zap ------------------------------------------------------ */
+/* Exact integer sums of (v-128)^p, p = 1..4, per raw channel: threads over channels (4 per
+ * thread with 32-bit loads when aligned), time split over blockIdx.y; 64-bit integer atomics
+ * make the totals independent of the order. */
+constexpr int SK_TCHUNK = 256;
+
+__global__ void __launch_bounds__(256) k_sk_sums(const uint8_t *__restrict__ raw, int C_raw, long n0,
+                                                int vec, unsigned long long *__restrict__ sums)
+{
+    const int per = vec ? 4 : 1;
+    const long c0 = ((long)blockIdx.x * blockDim.x + threadIdx.x) * per;
+    if (c0 >= C_raw) return;
+    const long t0 = (long)blockIdx.y * SK_TCHUNK, t1 = min(t0 + SK_TCHUNK, n0);
+    long long a[4][4] = {};
+    for (long t = t0; t < t1; t++) {
+        int v[4];
+        if (vec) {
+            const uchar4 q = *reinterpret_cast<const uchar4 *>(raw + t * C_raw + c0);
+            v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+        } else {
+            v[0] = raw[t * C_raw + c0];
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            if (k < per) {
+                const long long d = v[k] - 128, d2 = d * d;
+                a[k][0] += d;
+                a[k][1] += d2;
+                a[k][2] += d2 * d;
+                a[k][3] += d2 * d2;
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+        if (k < per)
+#pragma unroll
+            for (int p = 0; p < 4; p++)
+                atomicAdd(&sums[(size_t)p * C_raw + c0 + k], (unsigned long long)a[k][p]);
+}
+
+/* One CTA: moments -> skewness, excess kurtosis (double, each operation rounded as written)
+ * -> exact quartiles by a bitonic sort in shared memory -> mask of channels outside
+ * [Q1 - thr*R, Q3 + thr*R] for either statistic. */
+__global__ void __launch_bounds__(1024) k_sk_select(const unsigned long long *__restrict__ sums,
+                                                   int C, long n0, float thr,
+                                                   double *__restrict__ stats,
+                                                   uint8_t *__restrict__ mask, int P)
+{
+    extern __shared__ double srt[];
+    __shared__ double lo[2], hi[2];
+    const double n = (double)n0;
+    for (int c = threadIdx.x; c < C; c += blockDim.x) {
+        const double a = __ddiv_rn((double)(long long)sums[c], n);
+        const double b = __ddiv_rn((double)(long long)sums[(size_t)C + c], n);
+        const double cc = __ddiv_rn((double)(long long)sums[(size_t)2 * C + c], n);
+        const double d = __ddiv_rn((double)(long long)sums[(size_t)3 * C + c], n);
+        const double aa = __dmul_rn(a, a);
+        const double m2 = __dsub_rn(b, aa);
+        const double m3 = __dadd_rn(__dsub_rn(cc, __dmul_rn(__dmul_rn(3., a), b)), __dmul_rn(__dmul_rn(2., aa), a));
+        const double m4 = __dsub_rn(__dadd_rn(__dsub_rn(d, __dmul_rn(__dmul_rn(4., a), cc)),
+                                             __dmul_rn(__dmul_rn(6., aa), b)),
+                                   __dmul_rn(__dmul_rn(3., aa), aa));
+        double sk = 0., ku = 0.;
+        if (m2 > 0.) {
+            sk = __ddiv_rn(m3, __dmul_rn(m2, __dsqrt_rn(m2)));
+            ku = __dsub_rn(__ddiv_rn(m4, __dmul_rn(m2, m2)), 3.);
+        }
+        stats[c] = sk;
+        stats[(size_t)C + c] = ku;
+    }
+    __syncthreads();
+    for (int q = 0; q < 2; q++) {
+        for (int i = threadIdx.x; i < P; i += blockDim.x)
+            srt[i] = i < C ? stats[(size_t)q * C + i] : INFINITY;
+        __syncthreads();
+        for (int k = 2; k <= P; k <<= 1)
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int i = threadIdx.x; i < P; i += blockDim.x) {
+                    const int l = i ^ j;
+                    if (l > i) {
+                        const double x = srt[i], y = srt[l];
+                        const bool up = (i & k) == 0;
+                        if ((x > y) == up) {
+                            srt[i] = y;
+                            srt[l] = x;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        if (threadIdx.x == 0) {
+            const double q1 = srt[C / 4], q3 = srt[C - 1 - C / 4];
+            const double R = __dsub_rn(q3, q1);
+            lo[q] = __dsub_rn(q1, __dmul_rn((double)thr, R));
+            hi[q] = __dadd_rn(q3, __dmul_rn((double)thr, R));
+        }
+        __syncthreads();
+    }
+    for (int c = threadIdx.x; c < C; c += blockDim.x) {
+        const double sk = stats[c], ku = stats[(size_t)C + c];
+        mask[c] = (sk < lo[0] || sk > hi[0] || ku < lo[1] || ku > hi[1]) ? 1 : 0;
+    }
+}
+
 /* ---- unpack + downsample ------------------------------------------------------------- */
 constexpr int UP_TJ = 64; /* output channels per CTA */
 constexpr int UP_TI = 32; /* output samples per CTA */
@@ -64,7 +169,7 @@ constexpr int UP_TI = 32; /* output samples per CTA */
  * raw tile is staged in shared memory with 32-bit loads when the row pitch allows. */
 __global__ void __launch_bounds__(256) k_unpack(const uint8_t *__restrict__ raw, int C_raw, long n0,
                                                int td, int fd, float *__restrict__ x, long ldx,
-                                               int C, long N)
+                                               int C, long N, const uint8_t *__restrict__ mask)
 {
     extern __shared__ uint8_t tile[];
     __shared__ float outt[UP_TJ][UP_TI + 1];
@@ -103,9 +208,12 @@ __global__ void __launch_bounds__(256) k_unpack(const uint8_t *__restrict__ raw,
     for (int e = threadIdx.x; e < UP_TJ * UP_TI; e += blockDim.x) {
         int jj = e / UP_TI, ii = e % UP_TI;
         float acc = 0.f;
-        for (int k = 0; k < fd; k++)
+        for (int k = 0; k < fd; k++) {
+            const int c = c0 + jj * fd + k;
+            const bool z = mask && c < C_raw && mask[c];
             for (int t = 0; t < td; t++)
-                acc = __fadd_rn(acc, (float)tile[(ii * td + t) * cols + jj * fd + k]);
+                acc = __fadd_rn(acc, z ? 0.f : (float)tile[(ii * td + t) * cols + jj * fd + k]);
+        }
         outt[jj][ii] = acc;
     }
     __syncthreads();
@@ -119,20 +227,25 @@ __global__ void __launch_bounds__(256) k_unpack(const uint8_t *__restrict__ raw,
 
 /* fallback for large td*fd: one thread per output, no staging */
 __global__ void k_unpack_direct(const uint8_t *__restrict__ raw, int C_raw, int td, int fd,
-                                float *__restrict__ x, long ldx, int C, long N)
+                                float *__restrict__ x, long ldx, int C, long N,
+                                const uint8_t *__restrict__ mask)
 {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y;
     if (i >= N || j >= C) return;
     float acc = 0.f;
-    for (int k = 0; k < fd; k++)
+    for (int k = 0; k < fd; k++) {
+        const long c = (long)j * fd + k;
+        const bool z = mask && mask[c];
         for (int t = 0; t < td; t++)
-            acc = __fadd_rn(acc, (float)raw[(i * td + t) * (long)C_raw + (long)j * fd + k]);
+            acc = __fadd_rn(acc, z ? 0.f : (float)raw[(i * td + t) * (long)C_raw + c]);
+    }
     x[(long)j * ldx + i] = acc;
 }
 
 /* ---- equalize: exact integer statistics of the integer-valued downsampled block ---------- */
-__global__ void __launch_bounds__(256) k_equalize(float *__restrict__ x, long ldx, int C, long N)
+__global__ void __launch_bounds__(256) k_equalize(float *__restrict__ x, long ldx, int C, long N,
+                                                  uint8_t *__restrict__ live)
 {
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= C) return;
@@ -151,27 +264,56 @@ __global__ void __launch_bounds__(256) k_equalize(float *__restrict__ x, long ld
     double sd = var > 0. ? __dsqrt_rn(var) : 1.;
     const float mf = __double2float_rn(mean), inv = __double2float_rn(__ddiv_rn(1., sd));
     for (long i = lane; i < N; i += 32) r[i] = __fmul_rn(__fsub_rn(r[i], mf), inv);
+    if (live && lane == 0) live[w] = var > 0. ? 1 : 0;
 }
 
 /* ---- channel mean per sample (zero-DM series), sequential over channels ---------------- */
-__global__ void k_colmean(const float *__restrict__ x, long ldx, int C, long N,
-                          float *__restrict__ out)
+/* Channel sum per sample, in a fixed order: the channels are cut into CSUM_BLK consecutive
+ * blocks of ceil(C/CSUM_BLK); each block is summed sequentially from 0.0f (one warp per block,
+ * 32 samples per warp) and the block sums are added in block order.  Dead channels are
+ * exactly 0, so summing all channels equals summing the live ones; the divisor is the live
+ * count when `live` is given (BaseLine) and C otherwise (zdot). */
+constexpr int CSUM_BLK = 8;
+
+__global__ void __launch_bounds__(32 * CSUM_BLK) k_colmean(const float *__restrict__ x, long ldx, int C,
+                                                         long N, const uint8_t *__restrict__ live,
+                                                         float *__restrict__ out)
 {
-    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= N) return;
+    __shared__ float part[CSUM_BLK][32];
+    __shared__ int nlive_sh;
+    const int lane = threadIdx.x, q = threadIdx.y;
+    const long i = (long)blockIdx.x * 32 + lane;
+    const int cb = (C + CSUM_BLK - 1) / CSUM_BLK;
+    const int j0 = q * cb, j1 = min(C, j0 + cb);
     float acc = 0.f;
-    const float *p = x + i;
-    int j = 0;
-    for (; j + 4 <= C; j += 4) {
-        float a = p[(long)j * ldx], b = p[(long)(j + 1) * ldx], c = p[(long)(j + 2) * ldx],
-              d = p[(long)(j + 3) * ldx];
-        acc = __fadd_rn(acc, a);
-        acc = __fadd_rn(acc, b);
-        acc = __fadd_rn(acc, c);
-        acc = __fadd_rn(acc, d);
+    if (i < N) {
+        const float *p = x + i;
+        int j = j0;
+        for (; j + 8 <= j1; j += 8) {
+            float v[8];
+#pragma unroll
+            for (int r = 0; r < 8; r++) v[r] = p[(long)(j + r) * ldx];
+#pragma unroll
+            for (int r = 0; r < 8; r++) acc = __fadd_rn(acc, v[r]);
+        }
+        for (; j < j1; j++) acc = __fadd_rn(acc, p[(long)j * ldx]);
     }
-    for (; j < C; j++) acc = __fadd_rn(acc, p[(long)j * ldx]);
-    out[i] = __fdiv_rn(acc, (float)C);
+    part[q][lane] = acc;
+    if (q == 0 && lane == 0) {
+        int nl = C;
+        if (live) {
+            nl = 0;
+            for (int c = 0; c < C; c++) nl += live[c];
+        }
+        nlive_sh = nl;
+    }
+    __syncthreads();
+    if (q == 0 && i < N) {
+        float t = 0.f;
+#pragma unroll
+        for (int b = 0; b < CSUM_BLK; b++) t = __fadd_rn(t, part[b][lane]);
+        out[i] = nlive_sh > 0 ? __fdiv_rn(t, (float)nlive_sh) : 0.f;
+    }
 }
 
 __global__ void k_smooth(const float *__restrict__ z, long N, long nw, float *__restrict__ b)
@@ -186,11 +328,12 @@ __global__ void k_smooth(const float *__restrict__ z, long N, long nw, float *__
     b[i] = __fdiv_rn(acc, (float)(hi - lo + 1));
 }
 
-__global__ void k_sub_series(float *__restrict__ x, long ldx, long N, const float *__restrict__ b)
+__global__ void k_sub_series(float *__restrict__ x, long ldx, long N, const float *__restrict__ b,
+                             const uint8_t *__restrict__ live)
 {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y;
-    if (i >= N) return;
+    if (i >= N || (live && !live[j])) return;
     x[(long)j * ldx + i] = __fsub_rn(x[(long)j * ldx + i], b[i]);
 }
 
@@ -315,8 +458,29 @@ inline unsigned nblk(long n, int b) { return (unsigned)((n + b - 1) / b); }
 
 } // namespace
 
+size_t skzap_max_channels() { return 16384; }
+
+void launch_skzap(const uint8_t *raw, int C_raw, long n0, float thr, unsigned long long *sums,
+                  double *stats, uint8_t *mask, cudaStream_t st)
+{
+    cudaMemsetAsync(sums, 0, sizeof(unsigned long long) * 4 * (size_t)C_raw, st);
+    const int vec = (C_raw % 4 == 0) && ((reinterpret_cast<uintptr_t>(raw) & 3) == 0);
+    const long per_thread = vec ? 4 : 1;
+    dim3 g1(nblk((C_raw + per_thread - 1) / per_thread, 256), nblk(n0, SK_TCHUNK));
+    k_sk_sums<<<g1, 256, 0, st>>>(raw, C_raw, n0, vec, sums);
+    int P = 1;
+    while (P < C_raw) P <<= 1;
+    const size_t smem = (size_t)P * sizeof(double);
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_sk_select, cudaFuncAttributeMaxDynamicSharedMemorySize, 16384 * 8);
+        attr = true;
+    }
+    k_sk_select<<<1, 1024, smem, st>>>(sums, C_raw, n0, thr, stats, mask, P);
+}
+
 void launch_unpack(const uint8_t *raw, int C_raw, long n0, int td, int fd, float *x, long ldx,
-                   int C, long N, cudaStream_t st)
+                   int C, long N, const uint8_t *mask, cudaStream_t st)
 {
     size_t smem = (size_t)UP_TI * td * UP_TJ * fd;
     if (smem <= 96 * 1024) {
@@ -326,21 +490,22 @@ void launch_unpack(const uint8_t *raw, int C_raw, long n0, int td, int fd, float
             attr = true;
         }
         dim3 grid(nblk(N, UP_TI), nblk(C, UP_TJ));
-        k_unpack<<<grid, 256, smem, st>>>(raw, C_raw, n0, td, fd, x, ldx, C, N);
+        k_unpack<<<grid, 256, smem, st>>>(raw, C_raw, n0, td, fd, x, ldx, C, N, mask);
     } else {
         dim3 grid(nblk(N, 128), C);
-        k_unpack_direct<<<grid, 128, 0, st>>>(raw, C_raw, td, fd, x, ldx, C, N);
+        k_unpack_direct<<<grid, 128, 0, st>>>(raw, C_raw, td, fd, x, ldx, C, N, mask);
     }
 }
 
-void launch_equalize(float *x, long ldx, int C, long N, cudaStream_t st)
+void launch_equalize(float *x, long ldx, int C, long N, uint8_t *live, cudaStream_t st)
 {
-    k_equalize<<<nblk((long)C * 32, 256), 256, 0, st>>>(x, ldx, C, N);
+    k_equalize<<<nblk((long)C * 32, 256), 256, 0, st>>>(x, ldx, C, N, live);
 }
 
-void launch_colmean(const float *x, long ldx, int C, long N, float *out, cudaStream_t st)
+void launch_colmean(const float *x, long ldx, int C, long N, const uint8_t *live, float *out,
+                    cudaStream_t st)
 {
-    k_colmean<<<nblk(N, 128), 128, 0, st>>>(x, ldx, C, N, out);
+    k_colmean<<<nblk(N, 32), dim3(32, CSUM_BLK), 0, st>>>(x, ldx, C, N, live, out);
 }
 
 void launch_smooth(const float *z, long N, long nw, float *b, cudaStream_t st)
@@ -348,10 +513,11 @@ void launch_smooth(const float *z, long N, long nw, float *b, cudaStream_t st)
     k_smooth<<<nblk(N, 128), 128, 0, st>>>(z, N, nw, b);
 }
 
-void launch_sub_series(float *x, long ldx, int C, long N, const float *b, cudaStream_t st)
+void launch_sub_series(float *x, long ldx, int C, long N, const float *b, const uint8_t *live,
+                       cudaStream_t st)
 {
     dim3 grid(nblk(N, 256), C);
-    k_sub_series<<<grid, 256, 0, st>>>(x, ldx, N, b);
+    k_sub_series<<<grid, 256, 0, st>>>(x, ldx, N, b, live);
 }
 
 void launch_zero_rows(float *x, long ldx, const int32_t *rows, int nrows, long N,
@@ -380,7 +546,7 @@ void launch_kadane(float *x, long ldx, int C, long N, int tdk, int fdk, float th
 void launch_zdot(float *x, long ldx, int C, long N, float *s, double *sstats, cudaStream_t st)
 {
     k_zdot_norm<<<nblk((long)C * 32, 256), 256, 0, st>>>(x, ldx, C, N);
-    k_colmean<<<nblk(N, 128), 128, 0, st>>>(x, ldx, C, N, s);
+    k_colmean<<<nblk(N, 32), dim3(32, CSUM_BLK), 0, st>>>(x, ldx, C, N, nullptr, s);
     k_zdot_sstats<<<1, 32, 0, st>>>(s, N, sstats);
     k_zdot_fit<<<nblk((long)C * 32, 256), 256, 0, st>>>(x, ldx, C, N, s, sstats);
 }
