@@ -1,0 +1,232 @@
+/*
+ * transientx_gb300.hpp -- header-only C++ layer over the C ABI (transientx_gb300.h) with the
+ * host-side shapes of the reference's classes for the single-pulse path:
+ *   txgpu::SinglePulse  - the per-ddplan-row configuration members of SinglePulse
+ *                         (include/singlepulse.h:95-133, defaults singlepulse.cpp:18-65)
+ *   txgpu::parse_ddplan - ddplan rows "td fd dms ddm ndm snrloss maxw [rfi opts]"
+ *                         (singlepulse.cpp:407-456)
+ *   txgpu::Search       - prepare (SinglePulse::prepare, singlepulse.cpp:206-254) for all rows,
+ *                         run(block) (the block-loop body, dedisperse_fil.cpp:324-337)
+ *   txgpu::Search::cluster - Cluster<double>::run's candlist (cluster.cpp:63-161) as
+ *                         (idm, isamp, wn, S) tuples, the order CandPlot::plot consumes
+ * Errors from the C ABI become txgpu::Error exceptions on the C++ side only.
+ */
+#ifndef TRANSIENTX_GB300_HPP
+#define TRANSIENTX_GB300_HPP
+
+#include <cctype>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <tuple>
+#include <utility>
+#include <vector>
+
+#include "transientx_gb300.h"
+
+namespace txgpu {
+
+struct Error : std::runtime_error {
+    int status;
+    Error(int s, const std::string &what) : std::runtime_error(what), status(s) {}
+};
+
+inline void check(int rc, const char *what)
+{
+    if (rc != TXG_OK) throw Error(rc, std::string(what) + ": " + txg_strerror(rc));
+}
+
+struct SinglePulse {
+    int td = 1, fd = 1;
+    float bswidth = 0.1f;
+    std::vector<std::pair<double, double>> zaplist;
+    std::vector<std::vector<std::string>> rfilist;
+    double widthlimit = 50e-3;
+    float threKadaneF = 7.f;
+    double dms = 0., ddm = 1.;
+    long ndm = 200;
+    double overlap = 0.;
+    float minw = 1e-4f, maxw = 0.02f, snrloss = 0.1f;
+    bool iqr = false;
+    float thre = 7.f;
+    double radius_smearing = 1e-3;
+    int kvalue = 2, maxncand = 100, minpts = 5;
+    bool remove_cand_with_maxwidth = false;
+    int nsub = 0, dm_group = 0;
+    int id = 1;
+
+    txg_row to_c() const
+    {
+        txg_row r{};
+        r.td = td;
+        r.fd = fd;
+        r.bswidth = bswidth;
+        if (rfilist.size() > 8 || zaplist.size() > 16) throw Error(TXG_ERR_ARG, "too many rfi entries");
+        r.nrfi = (int32_t)rfilist.size();
+        for (size_t i = 0; i < rfilist.size(); i++) {
+            const auto &op = rfilist[i];
+            if (op[0] == "kadaneF" && op.size() >= 3) {
+                r.rfi_kind[i] = TXG_RFI_KADANEF;
+                r.rfi_td[i] = std::stoi(op[1]);
+                r.rfi_fd[i] = std::stoi(op[2]);
+            } else if (op[0] == "zdot") {
+                r.rfi_kind[i] = TXG_RFI_ZDOT;
+                r.rfi_td[i] = r.rfi_fd[i] = 1;
+            } else {
+                throw Error(TXG_ERR_UNSUPPORTED, "rfilist entry " + op[0] + " is not implemented");
+            }
+        }
+        r.nzap = (int32_t)zaplist.size();
+        for (size_t i = 0; i < zaplist.size(); i++) {
+            r.zap[i][0] = zaplist[i].first;
+            r.zap[i][1] = zaplist[i].second;
+        }
+        r.threKadaneF = threKadaneF;
+        r.widthlimit = widthlimit;
+        r.dms = dms;
+        r.ddm = ddm;
+        r.ndm = ndm;
+        r.overlap = overlap;
+        r.minw = minw;
+        r.maxw = maxw;
+        r.snrloss = snrloss;
+        r.iqr = iqr ? 1 : 0;
+        r.thre = thre;
+        r.nsub = nsub;
+        r.dm_group = dm_group;
+        return r;
+    }
+};
+
+/* rfi options of one ddplan line or of the -z command-line option */
+inline void parse_rfi(const std::vector<std::string> &t, size_t i, SinglePulse &sp)
+{
+    while (i < t.size()) {
+        if ((t[i] == "mask" || t[i] == "kadaneF" || t[i] == "kadaneT") && i + 2 < t.size()) {
+            sp.rfilist.push_back({t[i], t[i + 1], t[i + 2]});
+            i += 3;
+        } else if (t[i] == "zap" && i + 2 < t.size()) {
+            sp.zaplist.emplace_back(std::stod(t[i + 1]), std::stod(t[i + 2]));
+            i += 3;
+        } else if (t[i] == "zero" || t[i] == "zdot") {
+            sp.rfilist.push_back({t[i]});
+            i += 1;
+        } else {
+            i += 1;
+        }
+    }
+}
+
+inline std::vector<SinglePulse> parse_ddplan(const std::string &text, SinglePulse sp = SinglePulse())
+{
+    std::vector<SinglePulse> rows;
+    std::istringstream in(text);
+    std::string line;
+    int id = 0;
+    while (std::getline(in, line)) {
+        size_t a = line.find_first_not_of(" \t\r");
+        if (a == std::string::npos || !std::isdigit((unsigned char)line[a])) continue;
+        std::istringstream ls(line.substr(a));
+        std::vector<std::string> t;
+        for (std::string w; ls >> w;) t.push_back(w);
+        if (t.size() < 7) continue;
+        sp.td = std::stoi(t[0]);
+        sp.fd = std::stoi(t[1]);
+        sp.dms = std::stod(t[2]);
+        sp.ddm = std::stod(t[3]);
+        sp.ndm = std::stol(t[4]);
+        sp.snrloss = std::stof(t[5]);
+        sp.maxw = std::stof(t[6]);
+        parse_rfi(t, 7, sp);
+        sp.id = ++id;
+        rows.push_back(sp);
+    }
+    return rows;
+}
+
+class Search {
+public:
+    Search(const std::vector<SinglePulse> &rows, int nchans, double tsamp,
+           const std::vector<double> &freqs, long ndump, int nbeams = 1, int precision = TXG_PREC_FP32,
+           int flags = 0, float zapthre = 4.f)
+        : rows_(rows)
+    {
+        std::vector<txg_row> c;
+        for (const auto &r : rows) c.push_back(r.to_c());
+        txg_plan p{};
+        p.nchans = nchans;
+        p.tsamp = tsamp;
+        p.frequencies = freqs.data();
+        p.ndump = ndump;
+        p.nrows = (int32_t)c.size();
+        p.rows = c.data();
+        p.nbeams = nbeams;
+        p.precision = precision;
+        p.flags = flags;
+        p.zapthre = zapthre;
+        check(txg_create(&p, &h_), "txg_create");
+        ndump_ = ndump;
+    }
+    ~Search() { txg_destroy(h_); }
+    Search(const Search &) = delete;
+    Search &operator=(const Search &) = delete;
+
+    /* one block of raw 8-bit samples [ndump][nchans] */
+    void run(const uint8_t *block, int beam = 0) { push(txg_push_block(h_, beam, block, ndump_)); }
+    void run_device(const uint8_t *dev_block, int beam = 0)
+    {
+        push(txg_push_block_device(h_, beam, dev_block, ndump_));
+    }
+    void sync() { push(txg_sync(h_)); }
+
+    txg_row_info info(int row, int beam = 0) const
+    {
+        txg_row_info i;
+        check(txg_get_row_info(h_, beam, row, &i), "txg_get_row_info");
+        return i;
+    }
+
+    std::vector<txg_cand> candidates(int row, int beam = 0) const
+    {
+        int64_t n = 0;
+        txg_get_candidates(h_, beam, row, nullptr, 0, &n);
+        std::vector<txg_cand> out((size_t)n);
+        int rc = txg_get_candidates(h_, beam, row, out.data(), n, &n);
+        if (rc != TXG_OK && rc != TXG_ERR_OVERFLOW) check(rc, "txg_get_candidates");
+        out.resize(std::min<size_t>(out.size(), (size_t)n));
+        return out;
+    }
+
+    /* Cluster<double>::run candlist of the row's last block */
+    std::vector<std::tuple<long, long, int, float>> cluster(int row, int beam = 0) const
+    {
+        const txg_row_info i = info(row, beam);
+        const SinglePulse &sp = rows_[row];
+        std::vector<txg_cand> c = candidates(row, beam);
+        std::vector<txg_cand> out(std::max(1, sp.maxncand));
+        int64_t n = 0;
+        check(txg_cluster(c.data(), (int64_t)c.size(), i.dms, i.ddm, i.fmax, i.fmin, i.tsamp,
+                          sp.radius_smearing, sp.maxncand, sp.minpts,
+                          sp.remove_cand_with_maxwidth ? 1 : 0, i.maxwn, out.data(),
+                          (int64_t)out.size(), &n),
+              "txg_cluster");
+        std::vector<std::tuple<long, long, int, float>> list;
+        for (int64_t k = 0; k < n; k++) list.emplace_back(out[k].idm, out[k].isamp, out[k].wn, out[k].S);
+        return list;
+    }
+
+    txg_handle *handle() const { return h_; }
+
+private:
+    void push(int rc)
+    {
+        if (rc != TXG_OK && rc != TXG_ERR_OVERFLOW) check(rc, "txg_push_block");
+    }
+    std::vector<SinglePulse> rows_;
+    txg_handle *h_ = nullptr;
+    long ndump_ = 0;
+};
+
+} // namespace txgpu
+
+#endif /* TRANSIENTX_GB300_HPP */

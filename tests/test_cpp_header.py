@@ -1,0 +1,72 @@
+"""The C++ layer (include/transientx_gb300.hpp) compiles against the C ABI and links with the
+library; on a GPU it also runs a small search end to end."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+SRC = r'''
+#include <cstdio>
+#include <cstdlib>
+#include <cmath>
+#include "transientx_gb300.hpp"
+int main(int argc, char **argv) {
+    const int C = 64; const long N = 2048; const double tsamp = 256e-6;
+    std::vector<double> f(C);
+    for (int j = 0; j < C; j++) f[j] = 1500.0 - (j + 0.5) * 300.0 / C;
+    auto rows = txgpu::parse_ddplan("# td fd dms ddm ndm snrloss maxw\n1 1 0 1 100 0.1 0.02\n");
+    rows[0].nsub = 8;
+    if (argc < 2) { std::printf("parsed %zu rows\n", rows.size()); return 0; }
+    txgpu::Search s(rows, C, tsamp, f, N);
+    std::vector<uint8_t> raw(N * C);
+    unsigned long long z = 12345;
+    int found = 0;
+    for (int b = 0; b < 4; b++) {
+        for (long t = 0; t < N; t++)
+            for (int j = 0; j < C; j++) {
+                double g = 0; for (int k = 0; k < 12; k++) { z = z * 6364136223846793005ULL + 1442695040888963407ULL; g += (z >> 11) * (1.0 / 9007199254740992.0); }
+                double v = 128 + 12 * (g - 6);
+                long tt = b * N + t;
+                double d = 4.148741601e3 * 50.0 * (1.0 / (f[j] * f[j]) - 1.0 / (f[0] * f[0])) / tsamp;
+                if (tt >= 5000 + std::lround(d) && tt < 5008 + std::lround(d)) v += 30;
+                raw[t * C + j] = (uint8_t)std::fmin(255, std::fmax(0, std::floor(v + 0.5)));
+            }
+        s.run(raw.data());
+        s.sync();
+        if (s.info(0).gated) found += (int)s.cluster(0).size();
+    }
+    std::printf("clusters %d\n", found);
+    return found > 0 ? 0 : 1;
+}
+'''
+
+
+def _compile(tmp_path):
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    from transientx_gb300 import _build
+    _build.build()
+    src = tmp_path / "drop_in.cpp"
+    src.write_text(SRC)
+    exe = tmp_path / "drop_in"
+    lib = os.path.join(ROOT, "transientx_gb300")
+    subprocess.run(["g++", "-std=c++17", "-O2", str(src), "-I", os.path.join(ROOT, "include"),
+                    "-L", lib, "-ltxgpu", f"-Wl,-rpath,{lib}", "-o", str(exe)], check=True)
+    return exe
+
+
+def test_header_compiles_and_parses(tmp_path):
+    exe = _compile(tmp_path)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
+    assert "parsed 1 rows" in out
+
+
+@pytest.mark.gpu
+def test_header_end_to_end(tmp_path):
+    exe = _compile(tmp_path)
+    r = subprocess.run([str(exe), "run"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr

@@ -68,7 +68,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=min(8, max(1, len(jobs)))) as ex:
         list(ex.map(_run, jobs))
     if force or jobs or _stale(LIB, objs):
-        _run([nv, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"])
+        _run([nv, *ARCH, "-shared", "-cudart", "static", "-o", LIB, *objs])
     synth_src = os.path.join(CSRC, "synth.c")
     if force or _stale(SYNTH, [synth_src]):
         _run(["gcc", "-O3", "-std=gnu11", "-fPIC", "-fopenmp", "-ffp-contract=off", "-shared",
