@@ -183,6 +183,19 @@ int txg_cluster(const txg_cand *cands, int64_t n, double dms, double ddm, double
                 int32_t minpts, int32_t drop, int32_t maxwn, txg_cand *out, int64_t cap,
                 int64_t *nout);
 
+/* kadaneF (one rfilist entry) on a block already in device memory, allocating nothing.  It
+ * has no counterpart in the reference; it exists for callers that cannot call cudaMalloc
+ * while they run (real-time back ends with all memory reserved at start-up, frameworks that
+ * own GPU memory through their own pool).  x: device block [nchans][ldx], zapped windows set
+ * to 0 in place; ranges: device output [nchans/fd][4] as in txg_get_zap_ranges; thr2: squared
+ * S/N threshold; wnlimit: minimum window in downsampled samples; stream: cudaStream_t or
+ * NULL.  Its scratch is a fixed device array of 2^21 floats (8 MiB) that every GPU loading the
+ * library holds until exit: (nsamples/td)*(nchans/fd) above that returns TXG_ERR_ARG.  Calls
+ * share that array, so calls overlapping on the GPU race.  The first call on a device looks up
+ * the array's address; make it before any stream capture on that device. */
+int txg_kadaneF_noalloc(float *x, int64_t ldx, int32_t nchans, int64_t nsamples, int32_t td,
+                        int32_t fd, float thr2, int64_t wnlimit, int32_t *ranges, void *stream);
+
 /* Device time per kernel class accumulated since the last call (plan flag TXG_FLAG_TIMING),
  * measured with CUDA events on the handle's stream: ms[c] total milliseconds and launches[c]
  * number of launches of class c; classes 0 unpack, 1 preprocess+RFI, 2 stage 1,

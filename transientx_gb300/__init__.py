@@ -78,7 +78,7 @@ EXPORTS = [
     "txg_get_row_info", "txg_get_candidates", "txg_get_dense", "txg_get_timdata",
     "txg_get_block", "txg_get_zap_ranges", "txg_get_tables", "txg_width_ladder", "txg_boxcar",
     "txg_cluster", "txg_get_timing", "txg_get_stream", "txg_strerror", "txg_version",
-    "txg_describe_row", "txg_pop_result", "txg_get_mask",
+    "txg_describe_row", "txg_pop_result", "txg_get_mask", "txg_kadaneF_noalloc",
 ]
 
 _lib: Optional[C.CDLL] = None
@@ -120,6 +120,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.txg_get_timing.argtypes = [vp, vp, vp, C.c_int32]
     L.txg_get_stream.argtypes = [vp, C.POINTER(vp)]
     L.txg_get_mask.argtypes = [vp, C.c_int32, vp]
+    L.txg_kadaneF_noalloc.argtypes = [vp, C.c_int64, C.c_int32, C.c_int64, C.c_int32, C.c_int32,
+                                      C.c_float, C.c_int64, vp, vp]
     L.txg_pop_result.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(C.c_int64),
                                  C.POINTER(C.c_int32), vp, C.c_int64, C.POINTER(C.c_int64)]
     L.txg_describe_row.argtypes = [C.POINTER(txg_plan), C.c_int32, C.POINTER(txg_row_info), vp,

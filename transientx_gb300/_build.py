@@ -14,7 +14,7 @@ LIB = os.path.join(PKG, "libtxgpu.so")
 SYNTH = os.path.join(PKG, "libtxsynth.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SRC = ["txg_pre.cu", "txg_dedisp.cu", "txg_boxcar.cu", "txg_api.cu"]
+CU_SRC = ["txg_pre.cu", "txg_dedisp.cu", "txg_boxcar.cu", "txg_api.cu", "txg_noalloc.cu"]
 CPP_SRC = ["txg_plan.cpp", "txg_cluster.cpp"]
 
 

@@ -41,6 +41,8 @@ static int fail(int code, const std::string &msg)
     return code;
 }
 
+int set_arg_error(const std::string &msg) { return fail(TXG_ERR_ARG, msg); }
+
 static constexpr int NSLOT = 3;
 static constexpr long PREFETCH = 1 << 14; /* candidates copied back without waiting */
 static constexpr int NCLASS = 5;

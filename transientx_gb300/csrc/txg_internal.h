@@ -98,6 +98,7 @@ size_t boxcar_max_samples();
 
 namespace txg {
 int set_cuda_error(cudaError_t e, const char *expr, const char *file, int line);
+int set_arg_error(const std::string &msg);
 const char *last_error_text();
 } // namespace txg
 
