@@ -40,6 +40,8 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-blocks", type=int, default=2, help="timed oracle blocks (CPU baseline)")
+    ap.add_argument("--rows", default="", help="comma-separated ddplan rows to keep (profiling)")
+    ap.add_argument("--ndm", type=int, default=0, help="override ndm of every row (profiling)")
     return ap.parse_args()
 
 
@@ -184,6 +186,7 @@ def run_reference(args, wl):
 def run_ours(args, wl):
     import torch
     import transientx_gb300 as tx
+    import transientx_gb300.shard  # noqa: F401
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -218,13 +221,13 @@ def run_ours(args, wl):
     def drain(stats):
         for r in range(len(wl.rows)):
             while True:
-                res = s.pop_result(r)
-                if res is None:
+                out = s.pop_result(r, points=False)
+                if out is None:
                     break
-                _, gated, cands, n = res
-                if gated:
+                res = out[0]
+                if res.gated:
                     stats["work"] += infos[r].ndm * infos[r].nsamples
-                    stats["ncand"][r] += n
+                    stats["ncand"][r] += res.npoints
                     stats["gated"][r] += 1
                     stats["launches"] += launches_per_block(wl.rows[r], infos[r], True)
                 else:
@@ -286,51 +289,49 @@ def run_ours(args, wl):
             "class_algorithmic_GBps": {names[c]: (nb_total[c] / (cls_ms[c] / 1e3) / 1e9
                                                    if cls_ms[c] > 0 else None) for c in range(5)}}
 
+    s.close()
     e2e = None
     if not args.no_e2e:
+        # the public host-pointer path: pinned host blocks, H2D inside the timed region, and
+        # Cluster::run on every block inside the library while the device runs ahead
+        s = tx.Search(wl.rows, fil.nchans, fil.tsamp, fil.freqs, wl.ndump,
+                      precision=args.precision, flags=tx.FLAG_CLUSTER)
         hpin = host.numpy()
+
+        def pop_all(st):
+            for r in range(len(wl.rows)):
+                while True:
+                    out = s.pop_result(r, points=False)
+                    if out is None:
+                        break
+                    res, _, cl = out
+                    st["d2h"] += 8 + 16 * res.npoints
+                    if res.gated:
+                        st["work"] += infos[r].ndm * infos[r].nsamples
+                        st["clusters"] += len(cl)
 
         def step_host(st):
             for b in range(nblk):
                 s.push_block(hpin[b * wl.ndump:(b + 1) * wl.ndump])
-                for r in range(len(wl.rows)):
-                    while True:
-                        res = s.pop_result(r)
-                        if res is None:
-                            break
-                        _, gated, cands, n = res
-                        st["d2h"] += 8 + 16 * len(cands)
-                        if gated:
-                            st["work"] += infos[r].ndm * infos[r].nsamples
-                            s.cluster(r, cands=cands)
+                pop_all(st)
             s.sync(allow_overflow=True)
-            for r in range(len(wl.rows)):
-                while True:
-                    res = s.pop_result(r)
-                    if res is None:
-                        break
-                    _, gated, cands, n = res
-                    st["d2h"] += 8 + 16 * len(cands)
-                    if gated:
-                        st["work"] += infos[r].ndm * infos[r].nsamples
-                        s.cluster(r, cands=cands)
+            pop_all(st)
 
-        step_host(new_stats())
-        st = new_stats()
+        step_host({"work": 0, "d2h": 0, "clusters": 0})
+        st = {"work": 0, "d2h": 0, "clusters": 0}
         barrier()
-        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        f0.record(stream)
         t0 = time.perf_counter()
         for _ in range(args.steps):
             step_host(st)
-        f1.record(stream)
         barrier()
         wall = time.perf_counter() - t0
+        wall = tx.shard.max_over_ranks(wall, dist)
         e2e = {"value": st["work"] * world / wall, "unit": "DM-trial samples/s",
                "h2d_bytes_per_step": nblk * blk_bytes,
                "d2h_bytes_per_step": st["d2h"] // max(1, args.steps),
-               "includes": "H2D from pinned host memory, candidate read-back, host clustering"}
-    s.close()
+               "clusters_per_step": st["clusters"] / max(1, args.steps),
+               "includes": "H2D from pinned host memory, candidate read-back, Cluster::run per block"}
+        s.close()
 
     if rank != 0:
         return
@@ -361,6 +362,14 @@ def main():
     from transientx_gb300 import synth
     make = synth.WORKLOADS[args.workload]
     wl = make(nsamples=args.nsamples) if args.nsamples else make()
+    if args.rows:
+        keep = [int(r) for r in args.rows.split(",")]
+        wl.rows = [wl.rows[r] for r in keep]
+        wl.name += "_rows" + "-".join(map(str, keep))
+    if args.ndm:
+        for sp in wl.rows:
+            sp.ndm = args.ndm
+        wl.name += f"_ndm{args.ndm}"
     if args.impl == "reference":
         run_reference(args, wl)
     else:

@@ -44,7 +44,8 @@ typedef enum {
     TXG_FLAG_AVX2_TAIL = 1,    /* reproduce the -mavx2 build's per-width range of boxcar.cpp:264-279 */
     TXG_FLAG_DENSE = 2,        /* keep dense mxS/mxwn (Boxcar::mxS/mxwn, include/boxcar.h:40-41) */
     TXG_FLAG_KEEP_SERIES = 4,  /* keep preprocessed block and dedispersed series for inspection */
-    TXG_FLAG_TIMING = 8        /* bracket each kernel class with CUDA events (txg_get_timing) */
+    TXG_FLAG_TIMING = 8,       /* bracket each kernel class with CUDA events (txg_get_timing) */
+    TXG_FLAG_CLUSTER = 16      /* run Cluster::run on every gated block while harvesting it */
 } txg_flags;
 
 /* One ddplan row: the fields of SinglePulse that SinglePulse::prepare/run read
@@ -67,6 +68,10 @@ typedef struct {
     float thre;                /* S/N threshold (cluster.cpp:95) */
     int32_t nsub;              /* subbands; 0 = automatic */
     int32_t dm_group;          /* fine DMs per coarse DM; 0 = automatic */
+    double radius_smearing;    /* Cluster::run arguments (singlepulse.cpp:332): radius in s */
+    int32_t maxncand, minpts;
+    int32_t drop;              /* remove_cand_with_maxwidth */
+    int32_t pad;
 } txg_row;
 
 typedef struct {
@@ -128,13 +133,22 @@ int txg_get_row_info(txg_handle *h, int32_t beam, int32_t row, txg_row_info *out
 int txg_get_candidates(txg_handle *h, int32_t beam, int32_t row, txg_cand *out, int64_t cap,
                        int64_t *n);
 
+/* Outcome of one block of one (beam,row). */
+typedef struct {
+    int64_t counter;           /* the row's sample counter after the block (boxcar.cpp:160) */
+    int32_t gated;             /* the block produced boxcar output */
+    int32_t overflow;          /* more points than cand_capacity (points list truncated) */
+    int64_t npoints;           /* S > thre points (Cluster::run input, cluster.cpp:91-112) */
+    int64_t nclusters;         /* reported candidates (Cluster::run candlist), with
+                                * TXG_FLAG_CLUSTER */
+} txg_result;
+
 /* Per-block results in push order: pops the oldest harvested block of (beam,row) not yet
- * popped (up to 256 are kept; older ones are dropped).  *counter is the row's sample counter
- * after that block (Boxcar::counter, boxcar.cpp:160), *gated whether it produced boxcar
- * output, *n the number of S > thre points (written to out up to cap, sorted as in
- * txg_get_candidates).  Returns TXG_ERR_STATE when no block is waiting. */
-int txg_pop_result(txg_handle *h, int32_t beam, int32_t row, int64_t *counter, int32_t *gated,
-                   txg_cand *out, int64_t cap, int64_t *n);
+ * popped (up to 256 are kept; older ones are dropped).  Points are sorted as in
+ * txg_get_candidates and written up to pcap; clusters in Cluster::run's order up to ccap.
+ * Returns TXG_ERR_STATE when no block is waiting. */
+int txg_pop_result(txg_handle *h, int32_t beam, int32_t row, txg_result *res, txg_cand *points,
+                   int64_t pcap, txg_cand *clusters, int64_t ccap);
 
 /* Dense Boxcar::mxS / mxwn of the last block (plan flag TXG_FLAG_DENSE): [ndm][nsamples]. */
 int txg_get_dense(txg_handle *h, int32_t beam, int32_t row, float *mxS, int32_t *mxwn);

@@ -94,6 +94,10 @@ struct SinglePulse {
         r.thre = thre;
         r.nsub = nsub;
         r.dm_group = dm_group;
+        r.radius_smearing = radius_smearing;
+        r.maxncand = maxncand;
+        r.minpts = minpts;
+        r.drop = remove_cand_with_maxwidth ? 1 : 0;
         return r;
     }
 };

@@ -28,7 +28,7 @@ ERR_ARG, ERR_NOMEM, ERR_CUDA, ERR_OVERFLOW = -1, -2, -3, -4
 ERR_TIMEOUT, ERR_STATE, ERR_NODEVICE, ERR_UNSUPPORTED = -5, -6, -7, -8
 RFI_KADANEF, RFI_ZDOT = 1, 2
 PREC_FP32, PREC_BF16, PREC_FP16 = 0, 1, 2
-FLAG_AVX2_TAIL, FLAG_DENSE, FLAG_KEEP_SERIES, FLAG_TIMING = 1, 2, 4, 8
+FLAG_AVX2_TAIL, FLAG_DENSE, FLAG_KEEP_SERIES, FLAG_TIMING, FLAG_CLUSTER = 1, 2, 4, 8, 16
 PRECISIONS = {"fp32": PREC_FP32, "bf16": PREC_BF16, "fp16": PREC_FP16}
 
 
@@ -46,8 +46,14 @@ class txg_row(C.Structure):
         ("widthlimit", C.c_double), ("dms", C.c_double), ("ddm", C.c_double),
         ("ndm", C.c_int64), ("overlap", C.c_double), ("minw", C.c_float), ("maxw", C.c_float),
         ("snrloss", C.c_float), ("iqr", C.c_int32), ("thre", C.c_float), ("nsub", C.c_int32),
-        ("dm_group", C.c_int32),
+        ("dm_group", C.c_int32), ("radius_smearing", C.c_double), ("maxncand", C.c_int32),
+        ("minpts", C.c_int32), ("drop", C.c_int32), ("pad", C.c_int32),
     ]
+
+
+class txg_result(C.Structure):
+    _fields_ = [("counter", C.c_int64), ("gated", C.c_int32), ("overflow", C.c_int32),
+                ("npoints", C.c_int64), ("nclusters", C.c_int64)]
 
 
 class txg_plan(C.Structure):
@@ -122,8 +128,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.txg_get_mask.argtypes = [vp, C.c_int32, vp]
     L.txg_kadaneF_noalloc.argtypes = [vp, C.c_int64, C.c_int32, C.c_int64, C.c_int32, C.c_int32,
                                       C.c_float, C.c_int64, vp, vp]
-    L.txg_pop_result.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(C.c_int64),
-                                 C.POINTER(C.c_int32), vp, C.c_int64, C.POINTER(C.c_int64)]
+    L.txg_pop_result.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(txg_result), vp, C.c_int64,
+                                 vp, C.c_int64]
     L.txg_describe_row.argtypes = [C.POINTER(txg_plan), C.c_int32, C.POINTER(txg_row_info), vp,
                                    vp, vp, vp]
     _lib = L
@@ -193,6 +199,8 @@ class SinglePulse:
         r.minw, r.maxw, r.snrloss = self.minw, self.maxw, self.snrloss
         r.iqr, r.thre = int(self.iqr), self.thre
         r.nsub, r.dm_group = self.nsub, self.dm_group
+        r.radius_smearing, r.maxncand = self.radius_smearing, self.maxncand
+        r.minpts, r.drop = self.minpts, int(self.remove_cand_with_maxwidth)
         return r
 
 
@@ -348,21 +356,24 @@ class Search:
             _check(rc, "candidates")
         return out
 
-    def pop_result(self, row: int = 0, beam: int = 0):
-        """Oldest unread block of (beam,row): (counter, gated, candidates) or None."""
+    def pop_result(self, row: int = 0, beam: int = 0, points: bool = True):
+        """Oldest unread block of (beam,row) as (result, points, clusters), or None.  Clusters
+        are filled when the plan has FLAG_CLUSTER."""
         L = load_library()
-        cnt, gated, n = C.c_int64(), C.c_int32(), C.c_int64()
+        res = txg_result()
         buf = getattr(self, "_popbuf", None)
         if buf is None:
             buf = self._popbuf = np.zeros(self.cap, CAND_DTYPE)
-        rc = L.txg_pop_result(self.h, beam, row, C.byref(cnt), C.byref(gated), _ptr(buf),
-                              len(buf), C.byref(n))
+            self._clbuf = np.zeros(1 << 12, CAND_DTYPE)
+        rc = L.txg_pop_result(self.h, beam, row, C.byref(res), _ptr(buf) if points else None,
+                              len(buf) if points else 0, _ptr(self._clbuf), len(self._clbuf))
         if rc == ERR_STATE:
             return None
         if rc not in (OK, ERR_OVERFLOW):
             _check(rc, "pop_result")
-        m = min(n.value, self.cap)
-        return cnt.value, bool(gated.value), buf[:m].copy(), n.value
+        pts = buf[:min(res.npoints, self.cap)].copy() if points else None
+        cl = self._clbuf[:min(res.nclusters, len(self._clbuf))].copy()
+        return res, pts, cl
 
     def dense(self, row: int = 0, beam: int = 0) -> Tuple[np.ndarray, np.ndarray]:
         i = self.row_info(row, beam)

@@ -64,6 +64,7 @@ struct Result {
     int gated = 0;
     long count = 0;
     std::vector<txg_cand> cands;
+    std::vector<txg_cand> clusters;
 };
 
 struct BeamRow {
@@ -238,7 +239,7 @@ int harvest_slot(txg_handle *h, BeamRow &b, Slot &sl)
     return rc;
 }
 
-void enqueue(BeamRow &b)
+void enqueue(txg_handle *h, BeamRow &b, const RowPlan &P)
 {
     if (b.fifo.size() >= FIFO_MAX) b.fifo.pop_front();
     Result r;
@@ -246,14 +247,22 @@ void enqueue(BeamRow &b)
     r.gated = b.gated;
     r.count = b.last_count;
     r.cands = b.last;
+    if ((h->flags & TXG_FLAG_CLUSTER) && b.gated && !b.last.empty()) {
+        const txg_row &c = P.cfg;
+        r.clusters.resize(std::max(1, c.maxncand));
+        long m = cluster_run(b.last.data(), (long)b.last.size(), c.dms, c.ddm, P.fmax, P.fmin, P.tsamp,
+                             c.radius_smearing, c.maxncand, c.minpts, c.drop, P.maxwn, r.clusters.data(),
+                             (long)r.clusters.size());
+        r.clusters.resize(std::min<long>(m, (long)r.clusters.size()));
+    }
     b.fifo.push_back(std::move(r));
 }
 
-int harvest(txg_handle *h, BeamRow &b, Slot &sl)
+int harvest(txg_handle *h, BeamRow &b, Slot &sl, const RowPlan &P)
 {
     if (!sl.pending) return TXG_OK;
     int rc = harvest_slot(h, b, sl);
-    if (rc == TXG_OK || rc == TXG_ERR_OVERFLOW) enqueue(b);
+    if (rc == TXG_OK || rc == TXG_ERR_OVERFLOW) enqueue(h, b, P);
     return rc;
 }
 
@@ -282,7 +291,7 @@ int run_block(txg_handle *h, int beam, const uint8_t *raw)
         RowDev &D = h->rd[r];
         BeamRow &b = h->br[beam][r];
         Slot &sl = b.slot[b.nblocks % NSLOT];
-        int rc = harvest(h, b, sl);
+        int rc = harvest(h, b, sl, P);
         if (rc && rc != TXG_ERR_OVERFLOW) return rc;
         if (rc) status = rc;
         if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[0], h->st));
@@ -364,8 +373,10 @@ int finish_plan(RowPlan &P, int r)
     if (P.R < need) P.R = (need + 31) / 32 * 32;
     P.maxch = 0;
     for (int s = 0; s < P.nsub; s++) P.maxch = std::max(P.maxch, P.sub_start[s + 1] - P.sub_start[s]);
-    /* the stage-1 tile copy may read up to one tile past the block */
-    P.ldh = ((P.H + P.N + 256 + 16) + 31) / 32 * 32;
+    /* a stage-1 tile copy starts at most 3 columns before its tile and spans the 512-sample
+     * tile plus the largest within-subband delay plus alignment, so it may read up to
+     * H + N + 517 columns: pad the pitch past that */
+    P.ldh = ((P.H + P.N + 544) + 31) / 32 * 32;
     if ((size_t)P.nout > boxcar_max_samples())
         return fail(TXG_ERR_UNSUPPORTED, "row " + std::to_string(r) +
                                              ": ndump+noverlap exceeds the boxcar row limit of " +
@@ -602,11 +613,12 @@ int txg_sync(txg_handle *h)
     TXG_CUDA_TRY(cudaStreamSynchronize(h->st));
     int status = TXG_OK;
     for (auto &beam : h->br)
-        for (auto &b : beam) {
+        for (size_t r = 0; r < beam.size(); r++) {
+            BeamRow &b = beam[r];
             /* harvest in push order so `last` ends as the newest block */
             for (long k = b.nblocks - NSLOT; k < b.nblocks; k++) {
                 if (k < 0) continue;
-                int rc = harvest(h, b, b.slot[k % NSLOT]);
+                int rc = harvest(h, b, b.slot[k % NSLOT], h->rp[r]);
                 if (rc && (status == TXG_OK || status == TXG_ERR_OVERFLOW)) status = rc;
             }
         }
@@ -638,22 +650,30 @@ int txg_get_candidates(txg_handle *h, int32_t beam, int32_t row, txg_cand *out, 
     return b.last_count > h->cap ? TXG_ERR_OVERFLOW : TXG_OK;
 }
 
-int txg_pop_result(txg_handle *h, int32_t beam, int32_t row, int64_t *counter, int32_t *gated,
-                   txg_cand *out, int64_t cap, int64_t *n)
+int txg_pop_result(txg_handle *h, int32_t beam, int32_t row, txg_result *res, txg_cand *points,
+                   int64_t pcap, txg_cand *clusters, int64_t ccap)
 {
     int rc = check_beam_row(h, beam, row);
     if (rc) return rc;
     BeamRow &b = h->br[beam][row];
     if (b.fifo.empty()) return fail(TXG_ERR_STATE, "no block result waiting");
     Result &r = b.fifo.front();
-    if (counter) *counter = r.counter;
-    if (gated) *gated = r.gated;
-    if (n) *n = r.count;
-    if (out && cap > 0) {
-        long m = std::min<long>(cap, (long)r.cands.size());
-        if (m > 0) memcpy(out, r.cands.data(), m * sizeof(txg_cand));
-    }
     const bool over = r.count > h->cap;
+    if (res) {
+        res->counter = r.counter;
+        res->gated = r.gated;
+        res->overflow = over ? 1 : 0;
+        res->npoints = r.count;
+        res->nclusters = (int64_t)r.clusters.size();
+    }
+    if (points && pcap > 0) {
+        const long m = std::min<long>(pcap, (long)r.cands.size());
+        if (m > 0) memcpy(points, r.cands.data(), m * sizeof(txg_cand));
+    }
+    if (clusters && ccap > 0) {
+        const long m = std::min<long>(ccap, (long)r.clusters.size());
+        if (m > 0) memcpy(clusters, r.clusters.data(), m * sizeof(txg_cand));
+    }
     b.fifo.pop_front();
     return over ? TXG_ERR_OVERFLOW : TXG_OK;
 }

@@ -90,16 +90,47 @@ __device__ float select_kth(const float *row, long n, long k, unsigned *hist)
     return fkey_inv(prefix);
 }
 
+/* Best S over the width ladder for BX_U samples i = i0 + u*BX_THREADS.  CHECK selects the
+ * per-width range test (needed near the row ends); AVX2 reproduces the unordered-compare blend
+ * of the -mavx2 build. */
+template <bool CHECK, bool AVX2>
+__device__ __forceinline__ void widths_pass(const float *__restrict__ c, int i0, int n, int nw,
+                                            const int4 *__restrict__ wpar,
+                                            const float *__restrict__ temp_w, float *best, int *bw)
+{
+    for (int w = 0; w < nw; w++) {
+        const int4 p = wpar[w];
+        const float tw = temp_w[w];
+#pragma unroll
+        for (int u = 0; u < BX_U; u++) {
+            const int i = i0 + u * BX_THREADS;
+            if (!CHECK || (i >= p.x && i < p.z)) {
+                const float S = __fmul_rn(__fsub_rn(c[i + p.y], c[i - p.x]), tw);
+                if (S >= best[u]) {
+                    best[u] = S;
+                    bw[u] = p.w;
+                } else if (AVX2 && !(S < best[u])) {
+                    best[u] = 0.f;
+                    bw[u] = 0;
+                }
+            }
+        }
+    }
+}
+
+template <bool AVX2>
 __global__ void __launch_bounds__(BX_THREADS)
 k_boxcar(const float *__restrict__ tim, long ldt, long n, const int32_t *__restrict__ vwn,
-         int nw, int iqr, int avx2_tail, float thre, txg_cand *__restrict__ cand,
+         int nw, int iqr, float thre, txg_cand *__restrict__ cand,
          int *__restrict__ ncand, long cap, float *__restrict__ mxS, int32_t *__restrict__ mxwn)
 {
+    const int avx2_tail = AVX2 ? 1 : 0;
     extern __shared__ __align__(16) float c[];
     __shared__ double red[BX_THREADS / 32];
     __shared__ double chunk_off[BX_THREADS];
     __shared__ float temp_w[256];
     __shared__ int4 wpar[256]; /* wl, wh, end of the visited range, wn */
+    __shared__ int lo_all, hi_all; /* samples where every width is in range */
     __shared__ unsigned hist[256];
     __shared__ float mean_sh, var_sh;
     const long k = blockIdx.x;
@@ -197,9 +228,21 @@ k_boxcar(const float *__restrict__ tim, long ldt, long n, const int32_t *__restr
     }
     __syncthreads();
 
+    if (tid == 0) {
+        int lo = 0, hi = (int)n;
+        for (int w = 0; w < nw; w++) {
+            lo = max(lo, wpar[w].x);
+            hi = min(hi, wpar[w].z);
+        }
+        lo_all = lo;
+        hi_all = hi;
+    }
+    __syncthreads();
+
     const bool active = var > 0.f;
     const int lane = tid & 31;
-    for (long base = 0; base < n; base += (long)BX_THREADS * BX_U) {
+    const int nn = (int)n;
+    for (int base = 0; base < nn; base += BX_THREADS * BX_U) {
         float best[BX_U];
         int bw[BX_U];
 #pragma unroll
@@ -208,33 +251,20 @@ k_boxcar(const float *__restrict__ tim, long ldt, long n, const int32_t *__restr
             bw[u] = 0;
         }
         if (active) {
-            for (int w = 0; w < nw; w++) {
-                const int4 p = wpar[w];
-                const float tw = temp_w[w];
-#pragma unroll
-                for (int u = 0; u < BX_U; u++) {
-                    const long i = base + tid + (long)u * BX_THREADS;
-                    if (i >= p.x && i < p.z) {
-                        const float S = __fmul_rn(__fsub_rn(c[i + p.y], c[i - p.x]), tw);
-                        if (S >= best[u]) {
-                            best[u] = S;
-                            bw[u] = p.w;
-                        } else if (avx2_tail && !(S < best[u])) {
-                            best[u] = 0.f;
-                            bw[u] = 0;
-                        }
-                    }
-                }
-            }
+            const int i0 = base + tid;
+            if (base >= lo_all && base + BX_THREADS * BX_U <= hi_all)
+                widths_pass<false, AVX2>(c, i0, nn, nw, wpar, temp_w, best, bw);
+            else
+                widths_pass<true, AVX2>(c, i0, nn, nw, wpar, temp_w, best, bw);
         }
 #pragma unroll
         for (int u = 0; u < BX_U; u++) {
-            const long i = base + tid + (long)u * BX_THREADS;
-            if (i < n && mxS) {
+            const int i = base + tid + u * BX_THREADS;
+            if (i < nn && mxS) {
                 mxS[k * n + i] = best[u];
                 mxwn[k * n + i] = bw[u];
             }
-            const bool hit = i < n && best[u] > thre;
+            const bool hit = i < nn && best[u] > thre;
             const unsigned m = __ballot_sync(FULL, hit);
             if (m) {
                 int basei = 0;
@@ -261,9 +291,15 @@ int launch_boxcar(const float *tim, long ldt, long ndm, long n, const int32_t *v
     if (n <= 0 || ndm <= 0) return TXG_OK;
     if ((size_t)n > boxcar_max_samples() || nw > 256) return TXG_ERR_UNSUPPORTED;
     size_t smem = (size_t)n * sizeof(float);
-    cudaFuncSetAttribute(k_boxcar, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BX_SMEM_MAX);
-    k_boxcar<<<(unsigned)ndm, BX_THREADS, smem, st>>>(tim, ldt, n, vwn, nw, iqr, avx2_tail, thre,
-                                                      cand, ncand, cap, mxS, mxwn);
+    if (avx2_tail) {
+        cudaFuncSetAttribute(k_boxcar<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BX_SMEM_MAX);
+        k_boxcar<true><<<(unsigned)ndm, BX_THREADS, smem, st>>>(tim, ldt, n, vwn, nw, iqr, thre, cand,
+                                                                ncand, cap, mxS, mxwn);
+    } else {
+        cudaFuncSetAttribute(k_boxcar<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BX_SMEM_MAX);
+        k_boxcar<false><<<(unsigned)ndm, BX_THREADS, smem, st>>>(tim, ldt, n, vwn, nw, iqr, thre, cand,
+                                                                 ncand, cap, mxS, mxwn);
+    }
     return TXG_OK;
 }
 

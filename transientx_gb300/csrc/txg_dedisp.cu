@@ -190,16 +190,121 @@ k_stage1(const float *__restrict__ xh, long ldh, long col0, int C, long N, int n
     }
 }
 
+/* Stage 1 with the subband's whole channel window resident in shared memory: one CTA per
+ * (512-sample tile, subband) loads every channel row of the subband once (so each input
+ * element crosses HBM once per tile) and then walks all coarse-DM groups, 16 at a time.  Each
+ * output adds its channels in ascending order from 0.0f. */
+constexpr int S1R_THREADS = 256;
+constexpr int S1R_U = 2;
+constexpr int S1R_TT = S1R_THREADS * S1R_U;
+
+template <typename T>
+__global__ void __launch_bounds__(S1R_THREADS)
+k_stage1r(const float *__restrict__ xh, long ldh, long col0, int C, long N, int nsub, int ng,
+          const int32_t *__restrict__ sub_start, const int32_t *__restrict__ d1, long wmax,
+          int maxch, T *__restrict__ ring, long R, long tbase_mod, int *err)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ int span_sh;
+    float *win = reinterpret_cast<float *>(smraw);
+    int32_t *dsm = reinterpret_cast<int32_t *>(win + (size_t)maxch * wmax);
+    const int s = blockIdx.y;
+    const long u0 = (long)blockIdx.x * S1R_TT;
+    const int j0 = sub_start[s], j1 = sub_start[s + 1], jn = j1 - j0;
+    const int tid = threadIdx.x;
+    const long cstart = (u0 + col0) & ~3L;
+    const int al = (int)(u0 + col0 - cstart);
+
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+        span_sh = 0;
+    }
+    __syncthreads();
+    for (int jj = tid; jj < jn; jj += S1R_THREADS)
+        atomicMax(&span_sh, d1[(size_t)(ng - 1) * C + j0 + jj]);
+    __syncthreads();
+    const long W = ((long)S1R_TT + span_sh + al + 3) / 4 * 4; /* <= wmax */
+    if (tid == 0) {
+        const uint32_t bytes = (uint32_t)(W * sizeof(float));
+        mbar_expect_tx(&bar, bytes * (uint32_t)jn);
+        for (int jj = 0; jj < jn; jj++)
+            bulk_g2s(win + (size_t)jj * W, xh + (long)(j0 + jj) * ldh + cstart, bytes, &bar);
+    }
+    const bool ok = mbar_wait(&bar, 0);
+    if (!__syncthreads_and(ok)) {
+        if (tid == 0) atomicExch(err, 1);
+        mbar_wait(&bar, 0);
+        return;
+    }
+    for (int g0 = 0; g0 < ng; g0 += S1_GPC) {
+        const int gn = min(S1_GPC, ng - g0);
+        /* delays of the chunk; groups past the end repeat the last one (no reload) */
+        for (int e = tid; e < jn * S1_GPC; e += S1R_THREADS) {
+            const int jj = e / S1_GPC, g = e % S1_GPC;
+            dsm[e] = d1[(size_t)(g0 + (g < gn ? g : gn - 1)) * C + j0 + jj];
+        }
+        __syncthreads();
+        float acc[S1_GPC][S1R_U];
+#pragma unroll
+        for (int g = 0; g < S1_GPC; g++)
+#pragma unroll
+            for (int q = 0; q < S1R_U; q++) acc[g][q] = 0.f;
+        for (int jj = 0; jj < jn; jj++) {
+            const float *wr = win + (size_t)jj * W + al + tid;
+            const int4 *dv = reinterpret_cast<const int4 *>(dsm + jj * S1_GPC);
+            int dd[S1_GPC];
+#pragma unroll
+            for (int gq = 0; gq < S1_GPC / 4; gq++) {
+                const int4 d = dv[gq];
+                dd[4 * gq] = d.x;
+                dd[4 * gq + 1] = d.y;
+                dd[4 * gq + 2] = d.z;
+                dd[4 * gq + 3] = d.w;
+            }
+            float v[S1R_U];
+#pragma unroll
+            for (int q = 0; q < S1R_U; q++) v[q] = wr[dd[0] + q * S1R_THREADS];
+#pragma unroll
+            for (int g = 0; g < S1_GPC; g++) {
+                if (g > 0) {
+#pragma unroll
+                    for (int q = 0; q < S1R_U; q++) v[q] = wr[dd[g] + q * S1R_THREADS];
+                }
+#pragma unroll
+                for (int q = 0; q < S1R_U; q++) acc[g][q] = __fadd_rn(acc[g][q], v[q]);
+            }
+        }
+#pragma unroll
+        for (int g = 0; g < S1_GPC; g++) {
+            if (g < gn) {
+                T *out = ring + ((size_t)(g0 + g) * nsub + s) * R;
+#pragma unroll
+                for (int q = 0; q < S1R_U; q++) {
+                    const long u = u0 + tid + q * S1R_THREADS;
+                    if (u < N) {
+                        long t = tbase_mod + u;
+                        t = t >= R ? t - R : t;
+                        out[t] = to_store<T>(acc[g][q]);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
 /* ---- stage 2 ---------------------------------------------------------------------------- */
 constexpr int S2_THREADS = 128;
-constexpr int S2_U = 2;
+constexpr int S2_U = 2;                  /* samples per thread */
 constexpr int S2_TT = S2_THREADS * S2_U;
-constexpr int S2_KPC = 16;                    /* fine DMs per CTA (all in one group) */
 
-/* grid: x = time tiles, y = (group, DM chunk).  Shared memory: for a chunk of `sc` subbands
- * their ring windows (each S2_TT + d2[klast][s] - d2[kfirst][s] plus alignment), then the d2
- * offsets [sc][S2_KPC], the window starts [sc] and the copy parameters. */
-template <typename T>
+/* grid: x = time tiles, y = (group, DM chunk of KPC).  Shared memory: for a chunk of `sc`
+ * subbands their ring windows (each S2_TT + d2[klast][s] - d2[kfirst][s] plus alignment),
+ * then the d2 offsets [sc][KPC] and the window bookkeeping.  Each output adds its subbands
+ * in ascending order from 0.0f. */
+template <typename T, int KPC>
 __global__ void __launch_bounds__(S2_THREADS)
 k_stage2(const T *__restrict__ ring, long R, int nsub, int G, long ndm, long nout,
          const int32_t *__restrict__ d2, long t0_mod, int sc, long wtot_max,
@@ -209,14 +314,14 @@ k_stage2(const T *__restrict__ ring, long R, int nsub, int G, long ndm, long nou
     __shared__ __align__(8) uint64_t bar;
     T *win = reinterpret_cast<T *>(smraw);
     int32_t *doff = reinterpret_cast<int32_t *>(smraw + ((wtot_max * sizeof(T) + 15) / 16) * 16);
-    int32_t *wbeg = doff + sc * S2_KPC;
+    int32_t *wbeg = doff + sc * KPC;
     int32_t *wts = wbeg + sc, *wal = wts + sc, *wlen = wal + sc, *wpos = wlen + sc;
     const int tid = threadIdx.x;
-    const int nkc = (G + S2_KPC - 1) / S2_KPC;
+    const int nkc = (G + KPC - 1) / KPC;
     const int g = blockIdx.y / nkc, kc = blockIdx.y % nkc;
-    const long k0 = (long)g * G + (long)kc * S2_KPC;
+    const long k0 = (long)g * G + (long)kc * KPC;
     const long kend = min((long)(g + 1) * G, ndm);
-    const int kn = (int)min((long)S2_KPC, kend - k0);
+    const int kn = (int)min((long)KPC, kend - k0);
     if (kn <= 0) return;
     const long u0 = (long)blockIdx.x * S2_TT;
 
@@ -226,9 +331,9 @@ k_stage2(const T *__restrict__ ring, long R, int nsub, int G, long ndm, long nou
     }
     __syncthreads();
 
-    float acc[S2_KPC][S2_U];
+    float acc[KPC][S2_U];
 #pragma unroll
-    for (int k = 0; k < S2_KPC; k++)
+    for (int k = 0; k < KPC; k++)
 #pragma unroll
         for (int q = 0; q < S2_U; q++) acc[k][q] = 0.f;
 
@@ -236,10 +341,10 @@ k_stage2(const T *__restrict__ ring, long R, int nsub, int G, long ndm, long nou
     constexpr int EPC = 16 / (int)sizeof(T); /* elements per 16 bytes */
     for (int s0 = 0; s0 < nsub; s0 += sc) {
         const int sn = min(sc, nsub - s0);
-        for (int e = tid; e < sn * S2_KPC; e += S2_THREADS) {
-            int ss = e / S2_KPC, k = e % S2_KPC;
-            int lo = d2[(size_t)k0 * nsub + s0 + ss];
-            doff[e] = k < kn ? d2[(size_t)(k0 + k) * nsub + s0 + ss] - lo : 0;
+        for (int e = tid; e < sn * KPC; e += S2_THREADS) {
+            const int ss = e / KPC, k = e % KPC;
+            const int lo = d2[(size_t)k0 * nsub + s0 + ss];
+            doff[e] = d2[(size_t)(k0 + (k < kn ? k : kn - 1)) * nsub + s0 + ss] - lo;
         }
         /* window of each subband: ring start rounded down to 16 bytes, length, offset */
         for (int ss = tid; ss < sn; ss += S2_THREADS) {
@@ -296,29 +401,33 @@ k_stage2(const T *__restrict__ ring, long R, int nsub, int G, long ndm, long nou
         }
         for (int ss = 0; ss < sn; ss++) {
             const T *wr = win + wbeg[ss] + tid;
-            const int4 *dv = reinterpret_cast<const int4 *>(doff + ss * S2_KPC);
+            const int4 *dv = reinterpret_cast<const int4 *>(doff + ss * KPC);
+            int dd[KPC];
 #pragma unroll
-            for (int kq = 0; kq < S2_KPC / 4; kq++) {
+            for (int kq = 0; kq < KPC / 4; kq++) {
                 const int4 d = dv[kq];
-                const int dd[4] = {d.x, d.y, d.z, d.w};
-#pragma unroll
-                for (int r = 0; r < 4; r++)
-#pragma unroll
-                    for (int q = 0; q < S2_U; q++)
-                        acc[kq * 4 + r][q] =
-                            __fadd_rn(acc[kq * 4 + r][q], to_f(wr[dd[r] + q * S2_THREADS]));
+                dd[4 * kq] = d.x;
+                dd[4 * kq + 1] = d.y;
+                dd[4 * kq + 2] = d.z;
+                dd[4 * kq + 3] = d.w;
             }
+            /* DMs past the end of a partial group repeat the last offset; their sums are
+             * discarded, and no per-DM branch keeps all loads free to issue together */
+#pragma unroll
+            for (int k = 0; k < KPC; k++)
+#pragma unroll
+                for (int q = 0; q < S2_U; q++)
+                    acc[k][q] = __fadd_rn(acc[k][q], to_f(wr[dd[k] + q * S2_THREADS]));
         }
         __syncthreads();
     }
 #pragma unroll
-    for (int k = 0; k < S2_KPC; k++) {
+    for (int k = 0; k < KPC; k++) {
         if (k < kn) {
-            float *o = tim + (k0 + k) * ldt;
 #pragma unroll
             for (int q = 0; q < S2_U; q++) {
-                long u = u0 + tid + q * S2_THREADS;
-                if (u < nout) o[u] = acc[k][q];
+                const long u = u0 + tid + q * S2_THREADS;
+                if (u < nout) tim[(k0 + k) * ldt + u] = acc[k][q];
             }
         }
     }
@@ -326,16 +435,37 @@ k_stage2(const T *__restrict__ ring, long R, int nsub, int G, long ndm, long nou
 
 inline unsigned nblk(long n, int b) { return (unsigned)((n + b - 1) / b); }
 
-constexpr size_t SMEM_BUDGET = 100 * 1024; /* two CTAs per SM overlap copies and math */
+constexpr size_t SMEM_BUDGET = 100 * 1024;     /* two CTAs per SM overlap copies and math */
+constexpr size_t RESIDENT_BUDGET = 200 * 1024; /* whole-subband stage-1 windows */
 
 } // namespace
 
-/* Largest window any stage-1 CTA needs: S1_TT + maxd1 + alignment (delays grow with the
- * group index).  xh points at column 0 of the channel buffer; col0 = H - maxd1. */
+/* Largest window any stage-1 CTA needs: tile + maxd1 + alignment (delays grow with the
+ * group index).  xh points at column 0 of the channel buffer; col0 = H - maxd1.  When the
+ * widest subband's full window fits in shared memory the resident kernel reads every channel
+ * row once; otherwise the chunked kernel (channel chunks, 16 groups per CTA) is used. */
 void launch_stage1(const float *xh, long ldh, long col0, int C, long N, int nsub, int ng,
                    const int32_t *sub_start, const int32_t *d1, long maxd1, int maxch, void *ring,
                    long R, long tbase_mod, int prec, int *err, cudaStream_t st)
 {
+    const long wr = ((long)S1R_TT + maxd1 + 3 + 3) / 4 * 4;
+    const size_t smem_r = (size_t)maxch * wr * sizeof(float) + (size_t)maxch * S1_GPC * sizeof(int32_t);
+    if (smem_r <= RESIDENT_BUDGET) {
+        dim3 grid(nblk(N, S1R_TT), nsub);
+#define TXG_S1R(TY)                                                                                \
+    cudaFuncSetAttribute(k_stage1r<TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r);  \
+    k_stage1r<TY><<<grid, S1R_THREADS, smem_r, st>>>(xh, ldh, col0, C, N, nsub, ng, sub_start, d1, \
+                                                     wr, maxch, (TY *)ring, R, tbase_mod, err)
+        if (prec == TXG_PREC_BF16) {
+            TXG_S1R(__nv_bfloat16);
+        } else if (prec == TXG_PREC_FP16) {
+            TXG_S1R(__half);
+        } else {
+            TXG_S1R(float);
+        }
+#undef TXG_S1R
+        return;
+    }
     long wmax = ((long)S1_TT + maxd1 + 3 + 3) / 4 * 4;
     size_t per = wmax * sizeof(float) + S1_GPC * sizeof(int32_t);
     int cj = (int)((SMEM_BUDGET - 64) / per);
@@ -358,13 +488,17 @@ void launch_stage1(const float *xh, long ldh, long col0, int C, long N, int nsub
     }
 }
 
-/* Largest d2 spread inside one DM chunk, over all chunks and subbands. */
+/* DMs per stage-2 CTA for a group of G fine DMs (one chunk per group when G <= 32). */
+static int stage2_kpc(int G) { return G <= 8 ? 8 : G <= 16 ? 16 : G <= 24 ? 24 : 32; }
+
+/* Largest d2 spread inside one stage-2 DM chunk, over all chunks and subbands. */
 long stage2_span(const int32_t *d2h, int nsub, int G, long ndm)
 {
+    const long kpc = stage2_kpc(G);
     long span = 0;
     for (long g0 = 0; g0 < ndm; g0 += G)
-        for (long k0 = g0; k0 < min(g0 + (long)G, ndm); k0 += S2_KPC) {
-            long k1 = min(min(k0 + (long)S2_KPC, g0 + (long)G), ndm) - 1;
+        for (long k0 = g0; k0 < min(g0 + (long)G, ndm); k0 += kpc) {
+            long k1 = min(min(k0 + kpc, g0 + (long)G), ndm) - 1;
             for (int s = 0; s < nsub; s++) {
                 long d = (long)d2h[k1 * nsub + s] - d2h[k0 * nsub + s];
                 span = d > span ? d : span;
@@ -376,25 +510,38 @@ long stage2_span(const int32_t *d2h, int nsub, int G, long ndm)
 /* Ring length a stage-2 window may need (the ring must be longer, so a window wraps once). */
 long stage2_window(long span) { return (long)S2_TT + span + 16; }
 
-template <typename T>
+template <typename T, int KPC>
 static void stage2_impl(const void *ring, long R, int nsub, int G, long ndm, long nout,
                         const int32_t *d2, long span, long t0_mod, float *tim, long ldt, int *err,
                         cudaStream_t st)
 {
     const long epc = 16 / (long)sizeof(T);
     const long wlen = ((long)S2_TT + span + 2 * epc) / epc * epc;
-    const size_t per = wlen * sizeof(T) + S2_KPC * sizeof(int32_t) + 5 * sizeof(int32_t);
+    const size_t per = wlen * sizeof(T) + KPC * sizeof(int32_t) + 5 * sizeof(int32_t);
     int sc = (int)((SMEM_BUDGET - 64) / per);
     if (sc > nsub) sc = nsub;
     if (sc < 1) sc = 1;
     const long wtot = (long)sc * wlen;
-    const size_t smem = ((wtot * sizeof(T) + 15) / 16) * 16 + (size_t)sc * S2_KPC * 4 + (size_t)sc * 5 * 4;
-    const int nkc = (G + S2_KPC - 1) / S2_KPC;
+    const size_t smem = ((wtot * sizeof(T) + 15) / 16) * 16 + (size_t)sc * KPC * 4 + (size_t)sc * 5 * 4;
+    const int nkc = (G + KPC - 1) / KPC;
     const long ng = (ndm + G - 1) / G;
     dim3 grid(nblk(nout, S2_TT), (unsigned)(ng * nkc));
-    cudaFuncSetAttribute(k_stage2<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_stage2<T><<<grid, S2_THREADS, smem, st>>>((const T *)ring, R, nsub, G, ndm, nout, d2, t0_mod,
-                                                sc, wtot, tim, ldt, err);
+    cudaFuncSetAttribute(k_stage2<T, KPC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_stage2<T, KPC><<<grid, S2_THREADS, smem, st>>>((const T *)ring, R, nsub, G, ndm, nout, d2,
+                                                     t0_mod, sc, wtot, tim, ldt, err);
+}
+
+template <typename T>
+static void stage2_dispatch(const void *ring, long R, int nsub, int G, long ndm, long nout,
+                            const int32_t *d2, long span, long t0_mod, float *tim, long ldt,
+                            int *err, cudaStream_t st)
+{
+    switch (stage2_kpc(G)) {
+    case 8: stage2_impl<T, 8>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, err, st); break;
+    case 16: stage2_impl<T, 16>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, err, st); break;
+    case 24: stage2_impl<T, 24>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, err, st); break;
+    default: stage2_impl<T, 32>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, err, st); break;
+    }
 }
 
 void launch_stage2(const void *ring, long R, int nsub, int G, long ndm, long nout,
@@ -402,11 +549,11 @@ void launch_stage2(const void *ring, long R, int nsub, int G, long ndm, long nou
                    int *err, cudaStream_t st)
 {
     if (prec == TXG_PREC_BF16)
-        stage2_impl<__nv_bfloat16>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, err, st);
+        stage2_dispatch<__nv_bfloat16>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, err, st);
     else if (prec == TXG_PREC_FP16)
-        stage2_impl<__half>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, err, st);
+        stage2_dispatch<__half>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, err, st);
     else
-        stage2_impl<float>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, err, st);
+        stage2_dispatch<float>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, err, st);
 }
 
 } // namespace txg

@@ -53,8 +53,9 @@ static void subbands(int C, int nsub, const std::vector<double> &f, std::vector<
     }
 }
 
-/* Largest DM group whose within-subband smearing stays within one sample:
- * group*ddm/2 * max_s dmdelay(1, fref_s, flow_s) <= tsamp. */
+/* Largest DM group whose within-subband smearing stays within one sample,
+ * group*ddm/2 * max_s dmdelay(1, fref_s, flow_s) <= tsamp, rounded down to a multiple of 8
+ * when it is at least 8 (the stage-2 kernel handles 8, 16, 24 or 32 DMs of one group per CTA). */
 int auto_group(int C, int nsub, const std::vector<double> &freqs, double tsamp, double ddm,
                long ndm)
 {
@@ -68,6 +69,7 @@ int auto_group(int C, int nsub, const std::vector<double> &freqs, double tsamp, 
     }
     if (!(ddm * kmax > 0.)) return (int)(ndm < 1 ? 1 : (ndm > 1 << 30 ? 1 << 30 : ndm));
     double g = std::floor(2. * tsamp / (ddm * kmax));
+    if (g >= 8.) g = std::floor(g / 8.) * 8.;
     if (g < 1.) g = 1.;
     if (g > (double)ndm) g = (double)ndm;
     return (int)g;

@@ -97,36 +97,40 @@ __global__ void __launch_bounds__(256) k_sk_sums(const uint8_t *__restrict__ raw
                 atomicAdd(&sums[(size_t)p * C_raw + c0 + k], (unsigned long long)a[k][p]);
 }
 
-/* One CTA: moments -> skewness, excess kurtosis (double, each operation rounded as written)
- * -> exact quartiles by a bitonic sort in shared memory -> mask of channels outside
- * [Q1 - thr*R, Q3 + thr*R] for either statistic. */
-__global__ void __launch_bounds__(1024) k_sk_select(const unsigned long long *__restrict__ sums,
-                                                   int C, long n0, float thr,
-                                                   double *__restrict__ stats,
+/* Per channel: moments -> skewness and excess kurtosis (double, each operation rounded as
+ * written), one thread per channel. */
+__global__ void k_sk_stats(const unsigned long long *__restrict__ sums, int C, long n0,
+                           double *__restrict__ stats)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= C) return;
+    const double n = (double)n0;
+    const double a = __ddiv_rn((double)(long long)sums[c], n);
+    const double b = __ddiv_rn((double)(long long)sums[(size_t)C + c], n);
+    const double cc = __ddiv_rn((double)(long long)sums[(size_t)2 * C + c], n);
+    const double d = __ddiv_rn((double)(long long)sums[(size_t)3 * C + c], n);
+    const double aa = __dmul_rn(a, a);
+    const double m2 = __dsub_rn(b, aa);
+    const double m3 = __dadd_rn(__dsub_rn(cc, __dmul_rn(__dmul_rn(3., a), b)), __dmul_rn(__dmul_rn(2., aa), a));
+    const double m4 = __dsub_rn(__dadd_rn(__dsub_rn(d, __dmul_rn(__dmul_rn(4., a), cc)),
+                                         __dmul_rn(__dmul_rn(6., aa), b)),
+                               __dmul_rn(__dmul_rn(3., aa), aa));
+    double sk = 0., ku = 0.;
+    if (m2 > 0.) {
+        sk = __ddiv_rn(m3, __dmul_rn(m2, __dsqrt_rn(m2)));
+        ku = __dsub_rn(__ddiv_rn(m4, __dmul_rn(m2, m2)), 3.);
+    }
+    stats[c] = sk;
+    stats[(size_t)C + c] = ku;
+}
+
+/* One CTA: exact quartiles of skewness and kurtosis by a bitonic sort in shared memory ->
+ * mask of channels outside [Q1 - thr*R, Q3 + thr*R] for either statistic. */
+__global__ void __launch_bounds__(1024) k_sk_select(int C, float thr, const double *__restrict__ stats,
                                                    uint8_t *__restrict__ mask, int P)
 {
     extern __shared__ double srt[];
     __shared__ double lo[2], hi[2];
-    const double n = (double)n0;
-    for (int c = threadIdx.x; c < C; c += blockDim.x) {
-        const double a = __ddiv_rn((double)(long long)sums[c], n);
-        const double b = __ddiv_rn((double)(long long)sums[(size_t)C + c], n);
-        const double cc = __ddiv_rn((double)(long long)sums[(size_t)2 * C + c], n);
-        const double d = __ddiv_rn((double)(long long)sums[(size_t)3 * C + c], n);
-        const double aa = __dmul_rn(a, a);
-        const double m2 = __dsub_rn(b, aa);
-        const double m3 = __dadd_rn(__dsub_rn(cc, __dmul_rn(__dmul_rn(3., a), b)), __dmul_rn(__dmul_rn(2., aa), a));
-        const double m4 = __dsub_rn(__dadd_rn(__dsub_rn(d, __dmul_rn(__dmul_rn(4., a), cc)),
-                                             __dmul_rn(__dmul_rn(6., aa), b)),
-                                   __dmul_rn(__dmul_rn(3., aa), aa));
-        double sk = 0., ku = 0.;
-        if (m2 > 0.) {
-            sk = __ddiv_rn(m3, __dmul_rn(m2, __dsqrt_rn(m2)));
-            ku = __dsub_rn(__ddiv_rn(m4, __dmul_rn(m2, m2)), 3.);
-        }
-        stats[c] = sk;
-        stats[(size_t)C + c] = ku;
-    }
     __syncthreads();
     for (int q = 0; q < 2; q++) {
         for (int i = threadIdx.x; i < P; i += blockDim.x)
@@ -371,15 +375,23 @@ __global__ void k_kadane_scan(const float *__restrict__ ds, int Cds, long Nds, i
     if (j >= Cds) return;
     float bestp = -INFINITY, bestn = -INFINITY, curp = 0.f, curn = 0.f;
     long csp = 0, csn = 0, sp = 0, ep = -1, sn = 0, en = -1;
-    for (long i = 0; i < Nds; i++) {
-        float v = ds[i * Cds + j];
+    auto step = [&](long i, float v) {
         curp = __fadd_rn(curp, v);
         curn = __fadd_rn(curn, -v);
         if (curp > bestp) { bestp = curp; sp = csp; ep = i; }
         if (curn > bestn) { bestn = curn; sn = csn; en = i; }
         if (curp < 0.f) { curp = 0.f; csp = i + 1; }
         if (curn < 0.f) { curn = 0.f; csn = i + 1; }
+    };
+    long i = 0;
+    for (; i + 8 <= Nds; i += 8) { /* eight loads in flight, then the sequential scan */
+        float v[8];
+#pragma unroll
+        for (int r = 0; r < 8; r++) v[r] = ds[(i + r) * Cds + j];
+#pragma unroll
+        for (int r = 0; r < 8; r++) step(i + r, v[r]);
     }
+    for (; i < Nds; i++) step(i, ds[i * Cds + j]);
     const float var = (float)(tdk * fdk);
 #pragma unroll
     for (int p = 0; p < 2; p++) {
@@ -421,12 +433,25 @@ __global__ void __launch_bounds__(256) k_zdot_norm(float *__restrict__ x, long l
     for (long i = lane; i < N; i += 32) r[i] = __fmul_rn(__fsub_rn(r[i], mf), inv);
 }
 
-__global__ void k_zdot_sstats(const float *__restrict__ s, long N, double *__restrict__ out)
+/* se and ss of the zero-DM series by the fixed warp pattern; the series is first staged in
+ * shared memory by the whole CTA (when it fits) so the one reducing warp does not wait on
+ * serialised global loads. */
+constexpr int SST_MAX = 12288; /* floats staged (48 KB) */
+
+__global__ void __launch_bounds__(1024) k_zdot_sstats(const float *__restrict__ s, long N,
+                                                     double *__restrict__ out)
 {
-    const int lane = threadIdx.x & 31;
+    __shared__ float sm[SST_MAX];
+    const bool staged = N <= SST_MAX;
+    if (staged) {
+        for (long i = threadIdx.x; i < N; i += blockDim.x) sm[i] = s[i];
+        __syncthreads();
+    }
     if (threadIdx.x >= 32) return;
-    double se = red32<0>(s, nullptr, N, lane);
-    double ss = red32<1>(s, nullptr, N, lane);
+    const int lane = threadIdx.x;
+    const float *src = staged ? sm : s;
+    double se = red32<0>(src, nullptr, N, lane);
+    double ss = red32<1>(src, nullptr, N, lane);
     if (lane == 0) {
         out[0] = se;
         out[1] = ss;
@@ -476,7 +501,8 @@ void launch_skzap(const uint8_t *raw, int C_raw, long n0, float thr, unsigned lo
         cudaFuncSetAttribute(k_sk_select, cudaFuncAttributeMaxDynamicSharedMemorySize, 16384 * 8);
         attr = true;
     }
-    k_sk_select<<<1, 1024, smem, st>>>(sums, C_raw, n0, thr, stats, mask, P);
+    k_sk_stats<<<nblk(C_raw, 256), 256, 0, st>>>(sums, C_raw, n0, stats);
+    k_sk_select<<<1, 1024, smem, st>>>(C_raw, thr, stats, mask, P);
 }
 
 void launch_unpack(const uint8_t *raw, int C_raw, long n0, int td, int fd, float *x, long ldx,
@@ -547,7 +573,7 @@ void launch_zdot(float *x, long ldx, int C, long N, float *s, double *sstats, cu
 {
     k_zdot_norm<<<nblk((long)C * 32, 256), 256, 0, st>>>(x, ldx, C, N);
     k_colmean<<<nblk(N, 32), dim3(32, CSUM_BLK), 0, st>>>(x, ldx, C, N, nullptr, s);
-    k_zdot_sstats<<<1, 32, 0, st>>>(s, N, sstats);
+    k_zdot_sstats<<<1, 1024, 0, st>>>(s, N, sstats);
     k_zdot_fit<<<nblk((long)C * 32, 256), 256, 0, st>>>(x, ldx, C, N, s, sstats);
 }
 
