@@ -58,7 +58,7 @@ class Row(C.Structure):
         ("widthlimit", C.c_double), ("dms", C.c_double), ("ddm", C.c_double),
         ("ndm", C.c_long), ("overlap", C.c_double), ("nsub", C.c_int), ("group", C.c_int),
         ("minw", C.c_float), ("maxw", C.c_float), ("snrloss", C.c_float), ("iqr", C.c_int),
-        ("avx2_tail", C.c_int), ("thre", C.c_float), ("zapthre", C.c_float),
+        ("avx2_tail", C.c_int), ("thre", C.c_float), ("zapthre", C.c_float), ("fp64", C.c_int),
     ]
 
 
@@ -89,6 +89,7 @@ def make_row(**kw) -> Row:
     r.avx2_tail = int(kw.get("avx2_tail", False))
     r.thre = kw.get("thre", 7.0)
     r.zapthre = kw.get("zapthre", -1.0)
+    r.fp64 = int(kw.get("fp64", False))
     return r
 
 

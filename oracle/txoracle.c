@@ -466,6 +466,43 @@ void txo_boxcar_match(const float *tim, long n, const int *vwn, int nw, int iqr,
     free(csump);
 }
 
+/* FP64 reference of the boxcar: the same search with mean, variance, running sum and S in
+ * double (used to state the error of the float paths). */
+void txo_boxcar_match_f64(const double *tim, long n, const int *vwn, int nw, float *vS,
+                          int *vwnmax)
+{
+    double *c = (double *)malloc(sizeof(double) * (n > 0 ? n : 1));
+    double *best = (double *)calloc(n > 0 ? n : 1, sizeof(double));
+    memset(vwnmax, 0, sizeof(int) * n);
+    double mean = 0., var = 0.;
+    for (long i = 0; i < n; i++) {
+        mean += tim[i];
+        var += tim[i] * tim[i];
+    }
+    mean /= (double)n;
+    var = var / (double)n - mean * mean;
+    double acc = 0.;
+    for (long i = 0; i < n; i++) {
+        acc += tim[i] - mean;
+        c[i] = acc;
+    }
+    if (var > 0.)
+        for (int k = 0; k < nw; k++) {
+            int wn = vwn[k], wl = wn / 2 + 1, wh = (wn - 1) / 2;
+            double temp = sqrt(1. / ((double)wn * var));
+            for (long i = wl; i < n - wh; i++) {
+                double S = (c[i + wh] - c[i - wl]) * temp;
+                if (S >= best[i]) {
+                    best[i] = S;
+                    vwnmax[i] = wn;
+                }
+            }
+        }
+    for (long i = 0; i < n; i++) vS[i] = (float)best[i];
+    free(c);
+    free(best);
+}
+
 void txo_boxcar_run(const float *tim, long ndm, long n, const int *vwn, int nw, int iqr,
                     int avx2_tail, float *mxS, int *mxwn)
 {
@@ -669,6 +706,7 @@ struct txo_dedisp {
     double *freqs, *fref;
     int32_t *sub_start, *d1, *d2;
     float *hist, *ring, *tim;
+    double *ring64, *tim64; /* FP64 mode: sums kept in double */
     long ldh;
 };
 
@@ -748,8 +786,20 @@ void txo_dedisp_destroy(txo_dedisp *dd)
 {
     if (!dd) return;
     free(dd->freqs); free(dd->fref); free(dd->sub_start); free(dd->d1); free(dd->d2);
-    free(dd->hist); free(dd->ring); free(dd->tim); free(dd);
+    free(dd->hist); free(dd->ring); free(dd->tim); free(dd->ring64); free(dd->tim64); free(dd);
 }
+
+/* Switch the dedispersion sums to double (both stages); txo_dedisp_run then fills the double
+ * series returned by txo_dedisp_timdata64. */
+void txo_dedisp_set_fp64(txo_dedisp *dd)
+{
+    txo_dedisp_info *in = &dd->info;
+    if (dd->ring64) return;
+    dd->ring64 = (double *)calloc((size_t)in->ngroup * in->nsub * in->ring, sizeof(double));
+    dd->tim64 = (double *)calloc((size_t)in->ndm * in->nout, sizeof(double));
+}
+
+const double *txo_dedisp_timdata64(const txo_dedisp *dd) { return dd->tim64; }
 
 void txo_dedisp_get_info(const txo_dedisp *dd, txo_dedisp_info *info) { *info = dd->info; }
 
@@ -778,42 +828,79 @@ int txo_dedisp_run(txo_dedisp *dd, const float *x, long ldx)
         memcpy(dd->hist + (long)j * ldh + H, x + (long)j * ldx, sizeof(float) * N);
     in->counter += N;
     long tbase = in->counter - N - H; /* absolute time of stage-1 output column 0 */
-    /* Loops run channel (subband) outermost and time innermost so they vectorise; every
-     * output still sums its terms in ascending channel (subband) order from 0.0f. */
-#pragma omp parallel num_threads(nthr())
-    {
-        float *acc = (float *)malloc(sizeof(float) * (N > in->nout ? N : in->nout));
-#pragma omp for collapse(2) schedule(static)
-        for (int g = 0; g < ng; g++)
-            for (int s = 0; s < nsub; s++) {
-                float *out = dd->ring + ((size_t)g * nsub + s) * R;
-                const int32_t *d1 = dd->d1 + (size_t)g * nchan;
-                for (long u = 0; u < N; u++) acc[u] = 0.f;
-                for (int j = dd->sub_start[s]; j < dd->sub_start[s + 1]; j++) {
-                    const float *src = dd->hist + (long)j * ldh + d1[j];
-                    for (long u = 0; u < N; u++) acc[u] = acc[u] + src[u];
-                }
-                for (long u = 0; u < N; u++) out[pmod(tbase + u, R)] = acc[u];
-            }
-        free(acc);
-    }
     int gated = in->counter >= in->offset - in->noverlap + N;
-    if (gated) {
-        long t0 = in->counter - N - in->offset, nout = in->nout;
+    if (dd->ring64) {
+        /* FP64 reference: the same sums in double */
+#pragma omp parallel num_threads(nthr())
+        {
+            double *acc = (double *)malloc(sizeof(double) * N);
+#pragma omp for collapse(2) schedule(static)
+            for (int g = 0; g < ng; g++)
+                for (int s = 0; s < nsub; s++) {
+                    double *out = dd->ring64 + ((size_t)g * nsub + s) * R;
+                    const int32_t *d1 = dd->d1 + (size_t)g * nchan;
+                    for (long u = 0; u < N; u++) acc[u] = 0.;
+                    for (int j = dd->sub_start[s]; j < dd->sub_start[s + 1]; j++) {
+                        const float *src = dd->hist + (long)j * ldh + d1[j];
+                        for (long u = 0; u < N; u++) acc[u] += (double)src[u];
+                    }
+                    for (long u = 0; u < N; u++) out[pmod(tbase + u, R)] = acc[u];
+                }
+            free(acc);
+        }
+        if (gated) {
+            long t0 = in->counter - N - in->offset, nout = in->nout;
 #pragma omp parallel for num_threads(nthr()) schedule(static)
-        for (long k = 0; k < in->ndm; k++) {
-            int g = (int)(k / in->group);
-            const int32_t *d2 = dd->d2 + (size_t)k * nsub;
-            float *o = dd->tim + (size_t)k * nout;
-            for (long i = 0; i < nout; i++) o[i] = 0.f;
-            for (int s = 0; s < nsub; s++) {
-                const float *row = dd->ring + ((size_t)g * nsub + s) * R;
-                long t = pmod(t0 + d2[s], R), i = 0;
-                while (i < nout) { /* contiguous runs up to the ring end */
-                    long run = R - t < nout - i ? R - t : nout - i;
-                    for (long q = 0; q < run; q++) o[i + q] = o[i + q] + row[t + q];
-                    i += run;
-                    t = 0;
+            for (long k = 0; k < in->ndm; k++) {
+                int g = (int)(k / in->group);
+                const int32_t *d2 = dd->d2 + (size_t)k * nsub;
+                double *o = dd->tim64 + (size_t)k * nout;
+                for (long i = 0; i < nout; i++) o[i] = 0.;
+                for (int s = 0; s < nsub; s++) {
+                    const double *row = dd->ring64 + ((size_t)g * nsub + s) * R;
+                    for (long i = 0; i < nout; i++) o[i] += row[pmod(t0 + i + d2[s], R)];
+                }
+                float *of = dd->tim + (size_t)k * nout;
+                for (long i = 0; i < nout; i++) of[i] = (float)o[i];
+            }
+        }
+    } else {
+        /* Loops run channel (subband) outermost and time innermost so they vectorise; every
+         * output still sums its terms in ascending channel (subband) order from 0.0f. */
+    #pragma omp parallel num_threads(nthr())
+        {
+            float *acc = (float *)malloc(sizeof(float) * (N > in->nout ? N : in->nout));
+    #pragma omp for collapse(2) schedule(static)
+            for (int g = 0; g < ng; g++)
+                for (int s = 0; s < nsub; s++) {
+                    float *out = dd->ring + ((size_t)g * nsub + s) * R;
+                    const int32_t *d1 = dd->d1 + (size_t)g * nchan;
+                    for (long u = 0; u < N; u++) acc[u] = 0.f;
+                    for (int j = dd->sub_start[s]; j < dd->sub_start[s + 1]; j++) {
+                        const float *src = dd->hist + (long)j * ldh + d1[j];
+                        for (long u = 0; u < N; u++) acc[u] = acc[u] + src[u];
+                    }
+                    for (long u = 0; u < N; u++) out[pmod(tbase + u, R)] = acc[u];
+                }
+            free(acc);
+        }
+        if (gated) {
+            long t0 = in->counter - N - in->offset, nout = in->nout;
+    #pragma omp parallel for num_threads(nthr()) schedule(static)
+            for (long k = 0; k < in->ndm; k++) {
+                int g = (int)(k / in->group);
+                const int32_t *d2 = dd->d2 + (size_t)k * nsub;
+                float *o = dd->tim + (size_t)k * nout;
+                for (long i = 0; i < nout; i++) o[i] = 0.f;
+                for (int s = 0; s < nsub; s++) {
+                    const float *row = dd->ring + ((size_t)g * nsub + s) * R;
+                    long t = pmod(t0 + d2[s], R), i = 0;
+                    while (i < nout) { /* contiguous runs up to the ring end */
+                        long run = R - t < nout - i ? R - t : nout - i;
+                        for (long q = 0; q < run; q++) o[i + q] = o[i + q] + row[t + q];
+                        i += run;
+                        t = 0;
+                    }
                 }
             }
         }
@@ -873,6 +960,7 @@ txo_sp *txo_sp_create(const txo_row *row, int nchan, const double *freqs, double
         txo_sp_destroy(sp);
         return NULL;
     }
+    if (row->fp64) txo_dedisp_set_fp64(sp->dd);
     sp->nw = txo_width_ladder(row->minw, row->maxw, row->snrloss, sp->tsamp, sp->vwn, 256);
     long nout = sp->dd->info.nout;
     sp->mxS = (float *)calloc((size_t)row->ndm * nout, sizeof(float));
@@ -916,9 +1004,16 @@ int txo_sp_run(txo_sp *sp, const uint8_t *raw)
         }
     }
     int gated = txo_dedisp_run(sp->dd, sp->x, sp->ldx);
-    if (gated)
+    if (gated && row->fp64) {
+        const long nout = sp->dd->info.nout;
+#pragma omp parallel for num_threads(nthr()) schedule(dynamic, 4)
+        for (long k = 0; k < row->ndm; k++)
+            txo_boxcar_match_f64(sp->dd->tim64 + k * nout, nout, sp->vwn, sp->nw, sp->mxS + k * nout,
+                                 sp->mxwn + k * nout);
+    } else if (gated) {
         txo_boxcar_run(sp->dd->tim, row->ndm, sp->dd->info.nout, sp->vwn, sp->nw, row->iqr,
                        row->avx2_tail, sp->mxS, sp->mxwn);
+    }
     return gated;
 }
 

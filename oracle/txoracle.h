@@ -58,6 +58,8 @@ void txo_boxcar_match(const float *tim, long n, const int *vwn, int nw, int iqr,
                       int avx2_tail, float *vS, int *vwnmax);
 void txo_boxcar_run(const float *tim, long ndm, long n, const int *vwn, int nw, int iqr,
                     int avx2_tail, float *mxS, int *mxwn);
+void txo_boxcar_match_f64(const double *tim, long n, const int *vwn, int nw, float *vS,
+                          int *vwnmax);
 
 /* ---- threshold scan + clustering (cluster.cpp:63-161, clustering.h:26-100) ------------ */
 typedef struct {
@@ -90,6 +92,8 @@ void txo_dedisp_tables(const txo_dedisp *dd, int32_t *d1, int32_t *d2, int32_t *
                        double *fref);
 int txo_dedisp_run(txo_dedisp *dd, const float *x, long ldx);
 const float *txo_dedisp_timdata(const txo_dedisp *dd);
+void txo_dedisp_set_fp64(txo_dedisp *dd);
+const double *txo_dedisp_timdata64(const txo_dedisp *dd);
 
 /* ---- one ddplan row, the SinglePulse::run chain --------------------------------------- */
 enum { TXO_RFI_KADANEF = 1, TXO_RFI_ZDOT = 2 };
@@ -111,6 +115,7 @@ typedef struct {
     int iqr, avx2_tail;
     float thre;
     float zapthre;
+    int fp64; /* dedispersion sums and boxcar in double: the FP64 reference */
 } txo_row;
 
 typedef struct txo_sp txo_sp;

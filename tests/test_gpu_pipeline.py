@@ -159,3 +159,52 @@ def test_device_pointer_input_matches_host_input(tx):
                 np.testing.assert_array_equal(a.timdata(r), b.timdata(r))
     finally:
         cudart.cudaFree(dptr)
+
+
+def _peak_errors(S_gpu, W_gpu, S_ref, thre, tol):
+    """Relative S/N error at every point above threshold in the FP64 reference, and whether the
+    brightest point of each DM row (the peak a cluster would report) is the same sample, or a
+    sample the reference scores within tol of its maximum (a tie at that precision)."""
+    sel = S_ref > thre
+    rel = np.abs(S_gpu[sel] - S_ref[sel]) / S_ref[sel] if sel.any() else np.zeros(0)
+    rows = np.nonzero(sel.any(axis=1))[0]
+    same_peak = []
+    for r in rows:
+        a, b = int(np.argmax(S_gpu[r])), int(np.argmax(S_ref[r]))
+        same_peak.append(a == b or S_ref[r, a] >= S_ref[r, b] * (1 - tol))
+    return rel, np.array(same_peak, bool)
+
+
+@pytest.mark.parametrize("prec,bound", [("fp32", 1e-4), ("fp16", 1e-3), ("bf16", None)])
+def test_snr_error_against_fp64_oracle(tx, oracle, prec, bound):
+    """S/N at every point above threshold against the FP64 reference (dedispersion sums and
+    boxcar statistics in double): FP32 within 1e-4, FP16 storage within 1e-3, BF16 reported."""
+    fil, rows, ndump = small_workload()
+    rows = [rows[0]]
+    orow = oracle_rows(oracle, rows, fil, ndump, tx, zapthre=4.0)[0]
+    info = tx.describe_row(rows, 0, fil.nchans, fil.tsamp, fil.freqs, ndump)[0]
+    r64 = oracle.make_row(td=rows[0].td, fd=rows[0].fd, bswidth=rows[0].bswidth,
+                          rfi=rows[0].rfilist, widthlimit=rows[0].widthlimit, dms=rows[0].dms,
+                          ddm=rows[0].ddm, ndm=rows[0].ndm, nsub=info.nsub, group=info.dm_group,
+                          maxw=rows[0].maxw, thre=rows[0].thre, zapthre=4.0, fp64=True)
+    o64 = oracle.SinglePulseRow(r64, fil.freqs, fil.tsamp, ndump)
+    worst, npts = 0.0, 0
+    with tx.Search(rows, fil.nchans, fil.tsamp, fil.freqs, ndump, precision=prec,
+                   flags=tx.FLAG_DENSE, zapthre=4.0) as s:
+        for b in range(fil.nsamples // ndump):
+            raw = fil.generate(b * ndump, ndump)
+            s.push_block(raw)
+            s.sync()
+            if not o64.run(raw):
+                continue
+            S, W = s.dense(0)
+            rel, same = _peak_errors(S, W, o64.mxS(), rows[0].thre, bound or 0.0)
+            npts += len(rel)
+            if len(rel):
+                worst = max(worst, float(rel.max()))
+            if bound is not None:
+                assert same.all(), f"{prec}: a row's peak moved"
+    assert npts > 0, "the injected pulses should give points above threshold"
+    print(f"{prec}: {npts} points above threshold, max relative S/N error {worst:.2e}")
+    if bound is not None:
+        assert worst <= bound, (prec, worst)

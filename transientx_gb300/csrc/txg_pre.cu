@@ -56,6 +56,28 @@ __device__ __forceinline__ double red32(const float *__restrict__ x, const float
     return warp_sum_d(acc);
 }
 
+/* Two fixed-pattern reductions of one row in a single pass (same per-lane order as red32):
+ * MODE 1 -> (sum x, sum x*x), MODE 2 -> (sum x, sum x*y). */
+template <int MODE>
+__device__ __forceinline__ void red32x2(const float *__restrict__ x, const float *__restrict__ y,
+                                        long n, int lane, double &o1, double &o2)
+{
+    double a1 = 0., a2 = 0.;
+    long i = lane;
+    while (i < n) {
+        float r1 = 0.f, r2 = 0.f;
+        for (int r = 0; r < 8 && i < n; r++, i += 32) {
+            const float v = x[i];
+            r1 = __fadd_rn(r1, v);
+            r2 = __fadd_rn(r2, MODE == 1 ? __fmul_rn(v, v) : __fmul_rn(v, y[i]));
+        }
+        a1 = __dadd_rn(a1, (double)r1);
+        a2 = __dadd_rn(a2, (double)r2);
+    }
+    o1 = warp_sum_d(a1);
+    o2 = warp_sum_d(a2);
+}
+
 /* ---- skewness/kurtosis channel zap ------------------------------------------------------ */
 /* Exact integer sums of (v-128)^p, p = 1..4, per raw channel: threads over channels (4 per
  * thread with 32-bit loads when aligned), time split over blockIdx.y; 64-bit integer atomics
@@ -423,8 +445,8 @@ __global__ void __launch_bounds__(256) k_zdot_norm(float *__restrict__ x, long l
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= C) return;
     float *r = x + (long)w * ldx;
-    double s1 = red32<0>(r, nullptr, N, lane);
-    double s2 = red32<1>(r, nullptr, N, lane);
+    double s1, s2;
+    red32x2<1>(r, nullptr, N, lane, s1, s2);
     const double dn = (double)N;
     double mean = __ddiv_rn(s1, dn);
     double var = __dsub_rn(__ddiv_rn(s2, dn), __dmul_rn(mean, mean));
@@ -450,8 +472,8 @@ __global__ void __launch_bounds__(1024) k_zdot_sstats(const float *__restrict__ 
     if (threadIdx.x >= 32) return;
     const int lane = threadIdx.x;
     const float *src = staged ? sm : s;
-    double se = red32<0>(src, nullptr, N, lane);
-    double ss = red32<1>(src, nullptr, N, lane);
+    double se, ss;
+    red32x2<1>(src, nullptr, N, lane, se, ss);
     if (lane == 0) {
         out[0] = se;
         out[1] = ss;
@@ -465,8 +487,8 @@ __global__ void __launch_bounds__(256) k_zdot_fit(float *__restrict__ x, long ld
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= C) return;
     float *r = x + (long)w * ldx;
-    double xe = red32<0>(r, nullptr, N, lane);
-    double xs = red32<2>(r, s, N, lane);
+    double xe, xs;
+    red32x2<2>(r, s, N, lane, xe, xs);
     const double se = sst[0], ss = sst[1], dn = (double)N;
     double tmp = __dsub_rn(__dmul_rn(se, se), __dmul_rn(ss, dn));
     double alpha = 0., beta = 0.;
