@@ -113,6 +113,39 @@ def test_product_cluster_matches_oracle_random(tx, oracle):
             np.testing.assert_array_equal(a[f], b[f])
 
 
+def test_product_cluster_edge_geometry(tx, oracle):
+    """Component search (DM-row sweep, or the grid when many DM rows lie within one radius)
+    against the oracle's breadth-first growth: radii at multiples of the DM and sample steps,
+    many tied S values, input in arbitrary order, tiny DM steps."""
+    rng = np.random.default_rng(11)
+    for trial in range(160):
+        n = int(rng.integers(1, 2500))
+        idm = rng.integers(0, int(rng.choice([5, 60, 400])), n)
+        isamp = rng.integers(0, int(rng.choice([50, 400, 4000])), n)
+        _, u = np.unique(idm * 100000 + isamp, return_index=True)
+        idm, isamp = idm[u], isamp[u]
+        n = len(idm)
+        order = np.lexsort((isamp, idm)) if trial % 4 else rng.permutation(n)
+        c = np.zeros(n, tx.CAND_DTYPE)
+        c["idm"], c["isamp"] = idm[order], isamp[order]
+        c["wn"] = rng.integers(1, 9, n)
+        c["S"] = np.round(rng.uniform(7, 12, n), 1).astype(np.float32)
+        tsamp, ddm = 1e-4, float(rng.choice([1e-6, 0.01, 0.05, 0.1, 0.5]))
+        step = oracle.dmdelay(ddm, 1500.0, 1200.0) * 0.5
+        radius = float(rng.choice([1.5 * tsamp, 3 * tsamp, step, 2 * step, np.hypot(step, tsamp),
+                                   1e-3, 3e-3]))
+        args = (0.0, ddm, 1500.0, 1200.0, tsamp, radius, int(rng.choice([1, 7, 100, 100000])),
+                int(rng.choice([0, 2, 5, 30])), bool(trial % 2), 8)
+        a = tx.cluster(c, *args)
+        oc = np.zeros(n, oracle.CAND_DTYPE)
+        for f in ("idm", "isamp", "wn", "S"):
+            oc[f] = c[f]
+        b, _ = oracle.cluster(oc, *args)
+        assert len(a) == len(b), trial
+        for f in ("idm", "isamp", "wn", "S"):
+            np.testing.assert_array_equal(a[f], b[f], err_msg=f"trial {trial} {f}")
+
+
 def test_parse_ddplan(tx):
     text = "# td fd dms ddm ndm snrloss maxwidth(s)\n1 1 0.0 0.1 3344 0.1 0.1 zdot\n" \
            "2 1 334.4 0.2 1255 0.1 0.1 kadaneF 8 4\n"
