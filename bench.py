@@ -26,6 +26,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 ELEM = {"fp32": 4, "bf16": 2, "fp16": 2}
+ZAPTHRE = 4.0  # PreprocessLite skewness/kurtosis channel-zap threshold (transientx_fil default)
 
 
 def parse_args():
@@ -119,8 +120,11 @@ def launches_per_block(sp, info, gated):
         n += 3 if op[0] == "kadaneF" else 4
     n += 1  # stage 1
     if gated:
-        n += 2  # stage 2, boxcar
+        n += 3  # stage 2, boxcar, candidate read-back
     return n
+
+
+SKZAP_LAUNCHES = 3  # per block, all rows: moments, statistics, outlier selection
 
 
 # ---- reference arm / CPU baseline: the oracle port on the host cores ------------------------
@@ -140,7 +144,7 @@ def cpu_reference(wl, steps, warmup, timed_blocks=None, nthreads=0):
                      threKadaneF=sp.threKadaneF, widthlimit=sp.widthlimit, dms=sp.dms,
                      ddm=sp.ddm, ndm=sp.ndm, overlap=sp.overlap, nsub=info.nsub,
                      group=info.dm_group, minw=sp.minw, maxw=sp.maxw, snrloss=sp.snrloss,
-                     thre=sp.thre)
+                     thre=sp.thre, zapthre=ZAPTHRE)
     orow = O.SinglePulseRow(row, wl.fil.freqs, wl.fil.tsamp, wl.ndump)
     b = 0
     while True:  # fill the DM-delay history (not timed)
@@ -214,7 +218,7 @@ def run_ours(args, wl):
 
     flags = tx.FLAG_TIMING
     s = tx.Search(wl.rows, fil.nchans, fil.tsamp, fil.freqs, wl.ndump, precision=args.precision,
-                  flags=flags)
+                  flags=flags, zapthre=ZAPTHRE)
     infos = [s.row_info(r) for r in range(len(wl.rows))]
     stream = torch.cuda.ExternalStream(s.stream())
 
@@ -240,6 +244,7 @@ def run_ours(args, wl):
     def step_device(stats):
         for b in range(nblk):
             s.push_block_device(base + b * blk_bytes)
+            stats["launches"] += SKZAP_LAUNCHES if ZAPTHRE > 0 else 0
             drain(stats)
         s.sync(allow_overflow=True)
         drain(stats)
@@ -295,7 +300,7 @@ def run_ours(args, wl):
         # the public host-pointer path: pinned host blocks, H2D inside the timed region, and
         # Cluster::run on every block inside the library while the device runs ahead
         s = tx.Search(wl.rows, fil.nchans, fil.tsamp, fil.freqs, wl.ndump,
-                      precision=args.precision, flags=tx.FLAG_CLUSTER)
+                      precision=args.precision, flags=tx.FLAG_CLUSTER, zapthre=ZAPTHRE)
         hpin = host.numpy()
 
         def pop_all(st):

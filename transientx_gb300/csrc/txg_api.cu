@@ -7,14 +7,22 @@
  *   history copy -> unpack+downsample -> equalize -> baseline -> zap -> rfilist ops ->
  *   stage 1 (ring) -> [gate, boxcar.cpp:161] stage 2 -> boxcar+threshold -> async D2H.
  * Candidate buffers rotate over NSLOT slots per (beam,row) so the device runs ahead of the
- * host; a slot is harvested (sorted into Cluster::run order, cluster.cpp:91-112) before it
- * is reused and at txg_sync.
+ * host; a slot is harvested before it is reused and at txg_sync.  A read-back kernel writes
+ * each block's candidates into host-mapped pinned memory (two buffers per slot); sorting them
+ * into Cluster::run order (cluster.cpp:91-112) and clustering run on worker threads, so the
+ * launching thread only waits for the device.  Raw blocks from host memory are copied on a
+ * second stream, overlapping the previous block's kernels.
  */
 #include <algorithm>
+#include <condition_variable>
 #include <cstdio>
 #include <cstring>
 #include <deque>
+#include <functional>
+#include <memory>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "txg_internal.h"
@@ -44,14 +52,20 @@ static int fail(int code, const std::string &msg)
 int set_arg_error(const std::string &msg) { return fail(TXG_ERR_ARG, msg); }
 
 static constexpr int NSLOT = 3;
-static constexpr long PREFETCH = 1 << 14; /* candidates copied back without waiting */
+static constexpr long HCAP_MAX = 1 << 18; /* candidates read back into pinned memory per block */
 static constexpr int NCLASS = 5;
 
+struct Result;
+
 struct Slot {
-    txg_cand *dcand = nullptr; /* device [cap] */
-    int *dcount = nullptr;     /* device [2]: count, error code */
-    txg_cand *hcand = nullptr; /* pinned [PREFETCH] */
-    int *hcount = nullptr;     /* pinned [2] */
+    txg_cand *dcand = nullptr;              /* device [cap] */
+    int *dcount = nullptr;                  /* device [2]: count, error code */
+    txg_cand *hbuf[2] = {nullptr, nullptr}; /* pinned, host-mapped [hcap] */
+    txg_cand *hbuf_dev[2] = {nullptr, nullptr};
+    std::shared_ptr<Result> reader[2];      /* result whose sort may still read hbuf[i] */
+    int buf = 0;                            /* buffer of the pending block */
+    long uses = 0;
+    int *hcount = nullptr;                  /* pinned [2] */
     cudaEvent_t done = nullptr;
     cudaEvent_t ev[NCLASS + 1] = {};
     bool pending = false;
@@ -62,9 +76,91 @@ struct Slot {
 struct Result {
     long counter = 0;
     int gated = 0;
-    long count = 0;
-    std::vector<txg_cand> cands;
+    long count = 0;                /* points above threshold (may exceed the capacity) */
+    const txg_cand *src = nullptr; /* pinned read-back of the first nsrc points */
+    long nsrc = 0;
+    std::vector<txg_cand> tail;    /* points beyond the pinned read-back */
+    std::vector<txg_cand> cands;   /* (idm, isamp) order */
     std::vector<txg_cand> clusters;
+    bool failed = false;
+    bool ready = false; /* guarded by Workers::m */
+};
+using ResultP = std::shared_ptr<Result>;
+
+/* Worker threads for the host side of harvested blocks. */
+struct Workers {
+    std::mutex m;
+    std::condition_variable more, done;
+    std::deque<std::function<void()>> q;
+    std::vector<std::thread> th;
+    long inflight = 0;
+    bool stop = false;
+
+    void start(int n)
+    {
+        try {
+            for (int i = 0; i < n; i++) th.emplace_back([this] { loop(); });
+        } catch (...) { /* fewer threads; with none, jobs run on the caller */
+        }
+    }
+    void loop()
+    {
+        for (;;) {
+            std::function<void()> f;
+            {
+                std::unique_lock<std::mutex> lk(m);
+                more.wait(lk, [&] { return stop || !q.empty(); });
+                if (q.empty()) return;
+                f = std::move(q.front());
+                q.pop_front();
+            }
+            f();
+        }
+    }
+    void submit(std::function<void()> f)
+    {
+        {
+            std::lock_guard<std::mutex> lk(m);
+            inflight++;
+            if (!th.empty()) q.push_back(std::move(f));
+        }
+        if (th.empty()) f();
+        else more.notify_one();
+    }
+    void finish(Result &r)
+    {
+        {
+            std::lock_guard<std::mutex> lk(m);
+            r.ready = true;
+            inflight--;
+        }
+        done.notify_all();
+    }
+    void complete(Result &r) /* a result with nothing to do on a worker */
+    {
+        std::lock_guard<std::mutex> lk(m);
+        r.ready = true;
+    }
+    void wait(const Result &r)
+    {
+        std::unique_lock<std::mutex> lk(m);
+        done.wait(lk, [&] { return r.ready; });
+    }
+    void drain()
+    {
+        std::unique_lock<std::mutex> lk(m);
+        done.wait(lk, [&] { return inflight == 0; });
+    }
+    void shutdown()
+    {
+        {
+            std::lock_guard<std::mutex> lk(m);
+            stop = true;
+        }
+        more.notify_all();
+        for (auto &t : th) t.join();
+        th.clear();
+    }
 };
 
 struct BeamRow {
@@ -85,11 +181,11 @@ struct BeamRow {
     /* state of the most recently harvested block */
     long counter = 0;
     int gated = 0;
-    std::vector<txg_cand> last;
+    ResultP last;
     long last_count = 0;
     bool overflow = false;
     int dev_error = 0;
-    std::deque<Result> fifo;  /* harvested blocks not yet popped */
+    std::deque<ResultP> fifo; /* harvested blocks not yet popped */
 };
 
 static constexpr size_t FIFO_MAX = 256;
@@ -118,11 +214,14 @@ struct txg_handle {
     std::vector<std::vector<BeamRow>> br; /* [beam][row] */
     std::vector<BeamPrep> prep;           /* [beam] */
     cudaStream_t st = nullptr;
+    cudaStream_t cst = nullptr; /* host-to-device copies of raw blocks */
     uint8_t *raw[2] = {nullptr, nullptr};
     uint8_t *stage[2] = {nullptr, nullptr}; /* pinned staging for pageable host input */
-    cudaEvent_t raw_free[2] = {nullptr, nullptr};
+    cudaEvent_t raw_free[2] = {nullptr, nullptr};   /* kernels done with raw[i] */
+    cudaEvent_t raw_loaded[2] = {nullptr, nullptr}; /* raw[i] copied in */
     int raw_cur = 0;
-    long cap = 0;
+    long cap = 0, hcap = 0;
+    std::unique_ptr<Workers> pool;
     int prec = 0, flags = 0;
     double class_ms[NCLASS] = {0};
     long class_n[NCLASS] = {0};
@@ -173,10 +272,13 @@ size_t ring_elem(int prec) { return prec == TXG_PREC_FP32 ? 4 : 2; }
 void free_all(txg_handle *h)
 {
     if (h->st) cudaStreamSynchronize(h->st);
+    if (h->cst) cudaStreamSynchronize(h->cst);
+    if (h->pool) h->pool->shutdown();
     for (auto &beam : h->br)
         for (auto &b : beam)
             for (auto &sl : b.slot) {
-                if (sl.hcand) cudaFreeHost(sl.hcand);
+                for (int i = 0; i < 2; i++)
+                    if (sl.hbuf[i]) cudaFreeHost(sl.hbuf[i]);
                 if (sl.hcount) cudaFreeHost(sl.hcount);
                 if (sl.done) cudaEventDestroy(sl.done);
                 for (auto &e : sl.ev)
@@ -187,14 +289,78 @@ void free_all(txg_handle *h)
     for (int i = 0; i < 2; i++) {
         if (h->stage[i]) cudaFreeHost(h->stage[i]);
         if (h->raw_free[i]) cudaEventDestroy(h->raw_free[i]);
+        if (h->raw_loaded[i]) cudaEventDestroy(h->raw_loaded[i]);
     }
     if (h->st) cudaStreamDestroy(h->st);
+    if (h->cst) cudaStreamDestroy(h->cst);
     h->st = nullptr;
+    h->cst = nullptr;
 }
 
-/* Collect one slot: wait for its block, sort its candidates into Cluster::run order and
- * make them the row's last block. */
-int harvest_slot(txg_handle *h, BeamRow &b, Slot &sl)
+/* Candidates into (idm, isamp) order, the order of Cluster::run's threshold scan
+ * (cluster.cpp:91-112): stable counting passes by isamp, then by idm. */
+void sort_points(const txg_cand *a, long na, const txg_cand *b, long nb, long ndm, long nout,
+                 std::vector<txg_cand> &out)
+{
+    const long n = na + nb;
+    out.resize(n);
+    auto at = [&](long i) -> const txg_cand & { return i < na ? a[i] : b[i - na]; };
+    bool inrange = true;
+    for (long i = 0; i < n && inrange; i++) {
+        const txg_cand &c = at(i);
+        inrange = c.idm >= 0 && c.idm < ndm && c.isamp >= 0 && c.isamp < nout;
+    }
+    if (!inrange) {
+        for (long i = 0; i < n; i++) out[i] = at(i);
+        std::stable_sort(out.begin(), out.end(), [](const txg_cand &x, const txg_cand &y) {
+            return x.idm != y.idm ? x.idm < y.idm : x.isamp < y.isamp;
+        });
+        return;
+    }
+    std::vector<txg_cand> tmp(n);
+    std::vector<long> pos(std::max(ndm, nout) + 1);
+    std::fill(pos.begin(), pos.begin() + nout + 1, 0);
+    for (long i = 0; i < n; i++) pos[at(i).isamp + 1]++;
+    for (long k = 0; k < nout; k++) pos[k + 1] += pos[k];
+    for (long i = 0; i < n; i++) tmp[pos[at(i).isamp]++] = at(i);
+    std::fill(pos.begin(), pos.begin() + ndm + 1, 0);
+    for (long i = 0; i < n; i++) pos[tmp[i].idm + 1]++;
+    for (long k = 0; k < ndm; k++) pos[k + 1] += pos[k];
+    for (long i = 0; i < n; i++) out[pos[tmp[i].idm]++] = tmp[i];
+}
+
+/* Host side of one harvested block (on a worker thread): sort its points, cluster them. */
+void post_process(const txg_handle *h, const RowPlan &P, Result &r)
+{
+    try {
+        sort_points(r.src, r.nsrc, r.tail.data(), (long)r.tail.size(), P.cfg.ndm, P.nout, r.cands);
+        r.src = nullptr;
+        std::vector<txg_cand>().swap(r.tail);
+        if ((h->flags & TXG_FLAG_CLUSTER) && r.gated && !r.cands.empty()) {
+            const txg_row &c = P.cfg;
+            r.clusters.resize(std::max(1, c.maxncand));
+            long m = cluster_run(r.cands.data(), (long)r.cands.size(), c.dms, c.ddm, P.fmax, P.fmin,
+                                 P.tsamp, c.radius_smearing, c.maxncand, c.minpts, c.drop, P.maxwn,
+                                 r.clusters.data(), (long)r.clusters.size());
+            r.clusters.resize(std::min<long>(m, (long)r.clusters.size()));
+        }
+    } catch (...) {
+        r.failed = true;
+        r.cands.clear();
+        r.clusters.clear();
+    }
+}
+
+int result_status(const txg_handle *h, const Result &r)
+{
+    if (r.failed) return fail(TXG_ERR_NOMEM, "host memory exhausted while sorting candidates");
+    if (r.count > h->cap) return TXG_ERR_OVERFLOW;
+    return TXG_OK;
+}
+
+/* Collect one slot: wait for its block, take its candidates and hand them to a worker; the
+ * result becomes the row's last block and joins its queue. */
+int harvest(txg_handle *h, BeamRow &b, Slot &sl, const RowPlan &P)
 {
     if (!sl.pending) return TXG_OK;
     TXG_CUDA_TRY(cudaEventSynchronize(sl.done));
@@ -210,59 +376,49 @@ int harvest_slot(txg_handle *h, BeamRow &b, Slot &sl)
     }
     b.counter = sl.counter;
     b.gated = sl.gated;
-    b.last.clear();
+    auto r = std::make_shared<Result>();
+    r->counter = sl.counter;
+    r->gated = sl.gated;
+    b.last = r;
     b.last_count = 0;
     if (sl.hcount[1] != 0) {
         b.dev_error = sl.hcount[1];
+        h->pool->complete(*r);
         return fail(TXG_ERR_TIMEOUT, "a bounded device wait gave up (kernel code " +
                                          std::to_string(sl.hcount[1]) + ")");
     }
-    if (!sl.gated) return TXG_OK;
-    const long cnt = sl.hcount[0];
-    b.last_count = cnt;
-    const long keep = std::min(cnt, h->cap);
-    b.last.resize(keep);
-    const long pre = std::min(keep, PREFETCH);
-    if (pre > 0) memcpy(b.last.data(), sl.hcand, pre * sizeof(txg_cand));
-    if (keep > pre)
-        TXG_CUDA_TRY(cudaMemcpy(b.last.data() + pre, sl.dcand + pre, (keep - pre) * sizeof(txg_cand),
-                                cudaMemcpyDeviceToHost));
-    std::sort(b.last.begin(), b.last.end(), [](const txg_cand &x, const txg_cand &y) {
-        return x.idm != y.idm ? x.idm < y.idm : x.isamp < y.isamp;
-    });
     int rc = TXG_OK;
-    if (cnt > h->cap) {
-        b.overflow = true;
-        rc = fail(TXG_ERR_OVERFLOW, "candidate buffer overflow: " + std::to_string(cnt) +
-                                        " points above threshold, capacity " + std::to_string(h->cap));
+    if (sl.gated) {
+        const long cnt = sl.hcount[0];
+        r->count = cnt;
+        b.last_count = cnt;
+        const long keep = std::min(cnt, h->cap);
+        const long pre = std::min(keep, h->hcap);
+        r->src = sl.hbuf[sl.buf];
+        r->nsrc = pre;
+        sl.reader[sl.buf] = r;
+        if (keep > pre) {
+            r->tail.resize(keep - pre);
+            TXG_CUDA_TRY(cudaMemcpy(r->tail.data(), sl.dcand + pre, (keep - pre) * sizeof(txg_cand),
+                                    cudaMemcpyDeviceToHost));
+        }
+        if (cnt > h->cap) {
+            b.overflow = true;
+            rc = fail(TXG_ERR_OVERFLOW, "candidate buffer overflow: " + std::to_string(cnt) +
+                                            " points above threshold, capacity " + std::to_string(h->cap));
+        }
     }
-    return rc;
-}
-
-void enqueue(txg_handle *h, BeamRow &b, const RowPlan &P)
-{
     if (b.fifo.size() >= FIFO_MAX) b.fifo.pop_front();
-    Result r;
-    r.counter = b.counter;
-    r.gated = b.gated;
-    r.count = b.last_count;
-    r.cands = b.last;
-    if ((h->flags & TXG_FLAG_CLUSTER) && b.gated && !b.last.empty()) {
-        const txg_row &c = P.cfg;
-        r.clusters.resize(std::max(1, c.maxncand));
-        long m = cluster_run(b.last.data(), (long)b.last.size(), c.dms, c.ddm, P.fmax, P.fmin, P.tsamp,
-                             c.radius_smearing, c.maxncand, c.minpts, c.drop, P.maxwn, r.clusters.data(),
-                             (long)r.clusters.size());
-        r.clusters.resize(std::min<long>(m, (long)r.clusters.size()));
-    }
-    b.fifo.push_back(std::move(r));
-}
-
-int harvest(txg_handle *h, BeamRow &b, Slot &sl, const RowPlan &P)
-{
-    if (!sl.pending) return TXG_OK;
-    int rc = harvest_slot(h, b, sl);
-    if (rc == TXG_OK || rc == TXG_ERR_OVERFLOW) enqueue(h, b, P);
+    b.fifo.push_back(r);
+    Workers *pool = h->pool.get();
+    const RowPlan *pp = &P;
+    if (r->nsrc > 0 || !r->tail.empty())
+        pool->submit([h, pool, pp, r] {
+            post_process(h, *pp, *r);
+            pool->finish(*r);
+        });
+    else
+        pool->complete(*r);
     return rc;
 }
 
@@ -346,8 +502,14 @@ int run_block(txg_handle *h, int beam, const uint8_t *raw)
             if (rc) return rc;
             TXG_CUDA_TRY(cudaGetLastError());
             if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[5], h->st));
-            TXG_CUDA_TRY(cudaMemcpyAsync(sl.hcand, sl.dcand, std::min(PREFETCH, h->cap) * sizeof(txg_cand),
-                                         cudaMemcpyDeviceToHost, h->st));
+            /* the buffer's previous reader (two uses of this slot ago) must be done */
+            sl.buf = (int)(sl.uses++ & 1);
+            if (sl.reader[sl.buf]) {
+                h->pool->wait(*sl.reader[sl.buf]);
+                sl.reader[sl.buf].reset();
+            }
+            launch_copy_cands(sl.dcand, sl.dcount, h->hcap, sl.hbuf_dev[sl.buf], h->st);
+            TXG_CUDA_TRY(cudaGetLastError());
         } else if (timing) {
             TXG_CUDA_TRY(cudaEventRecord(sl.ev[4], h->st));
             TXG_CUDA_TRY(cudaEventRecord(sl.ev[5], h->st));
@@ -470,6 +632,7 @@ int txg_create(const txg_plan *plan, txg_handle **out)
     h->prec = plan->precision;
     h->flags = plan->flags;
     h->cap = plan->cand_capacity > 0 ? plan->cand_capacity : (1L << 20);
+    h->hcap = std::min(h->cap, HCAP_MAX);
     int rc = TXG_OK;
     h->rp.resize(plan->nrows);
     for (int r = 0; r < plan->nrows && !rc; r++) {
@@ -489,6 +652,16 @@ int txg_create(const txg_plan *plan, txg_handle **out)
         delete h;
         return fail(TXG_ERR_CUDA, "cudaStreamCreate failed");
     }
+    if (cudaStreamCreateWithFlags(&h->cst, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaStreamDestroy(h->st);
+        delete h;
+        return fail(TXG_ERR_CUDA, "cudaStreamCreate failed");
+    }
+    h->pool.reset(new Workers());
+    {
+        const unsigned hw = std::thread::hardware_concurrency();
+        h->pool->start((int)std::max(1u, std::min(4u, hw / 2)));
+    }
     auto bail = [&](int code) {
         free_all(h);
         delete h;
@@ -499,7 +672,8 @@ int txg_create(const txg_plan *plan, txg_handle **out)
         if ((rc = dalloc(h, &h->raw[i], raw_bytes))) return bail(rc);
         if (cudaHostAlloc((void **)&h->stage[i], raw_bytes, cudaHostAllocDefault) != cudaSuccess)
             return bail(fail(TXG_ERR_NOMEM, "pinned staging allocation failed"));
-        if (cudaEventCreateWithFlags(&h->raw_free[i], cudaEventDisableTiming) != cudaSuccess)
+        if (cudaEventCreateWithFlags(&h->raw_free[i], cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&h->raw_loaded[i], cudaEventDisableTiming) != cudaSuccess)
             return bail(fail(TXG_ERR_CUDA, "event creation failed"));
     }
     h->rd.resize(plan->nrows);
@@ -549,10 +723,15 @@ int txg_create(const txg_plan *plan, txg_handle **out)
             for (auto &sl : b.slot) {
                 if ((rc = dalloc(h, &sl.dcand, (size_t)h->cap)) || (rc = dalloc(h, &sl.dcount, (size_t)2)))
                     return bail(rc);
-                if (cudaHostAlloc((void **)&sl.hcand, sizeof(txg_cand) * std::min(PREFETCH, h->cap),
-                                  cudaHostAllocDefault) != cudaSuccess ||
-                    cudaHostAlloc((void **)&sl.hcount, 2 * sizeof(int), cudaHostAllocDefault) != cudaSuccess)
-                    return bail(fail(TXG_ERR_NOMEM, "pinned candidate buffer allocation failed"));
+                for (int i = 0; i < 2; i++) {
+                    if (cudaHostAlloc((void **)&sl.hbuf[i], sizeof(txg_cand) * h->hcap, cudaHostAllocMapped) !=
+                        cudaSuccess)
+                        return bail(fail(TXG_ERR_NOMEM, "pinned candidate buffer allocation failed"));
+                    if (cudaHostGetDevicePointer((void **)&sl.hbuf_dev[i], sl.hbuf[i], 0) != cudaSuccess)
+                        return bail(fail(TXG_ERR_CUDA, "pinned candidate buffer is not device-mapped"));
+                }
+                if (cudaHostAlloc((void **)&sl.hcount, 2 * sizeof(int), cudaHostAllocDefault) != cudaSuccess)
+                    return bail(fail(TXG_ERR_NOMEM, "pinned count allocation failed"));
                 sl.hcount[0] = sl.hcount[1] = 0;
                 if (cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) != cudaSuccess)
                     return bail(fail(TXG_ERR_CUDA, "event creation failed"));
@@ -591,17 +770,22 @@ int txg_push_block(txg_handle *h, int32_t beam, const uint8_t *host, int64_t nsa
     const size_t bytes = (size_t)nsamp * h->plan.nchans;
     const int i = h->raw_cur;
     h->raw_cur ^= 1;
-    /* the device buffer (and staging) of two blocks ago must be consumed */
-    TXG_CUDA_TRY(cudaEventSynchronize(h->raw_free[i]));
     cudaPointerAttributes attr;
     const bool pinned = cudaPointerGetAttributes(&attr, host) == cudaSuccess &&
                         (attr.type == cudaMemoryTypeHost || attr.type == cudaMemoryTypeManaged);
     const uint8_t *src = host;
     if (!pinned) {
+        /* the staging buffer's previous copy (two blocks ago) must be done */
+        TXG_CUDA_TRY(cudaEventSynchronize(h->raw_loaded[i]));
         memcpy(h->stage[i], host, bytes);
         src = h->stage[i];
     }
-    TXG_CUDA_TRY(cudaMemcpyAsync(h->raw[i], src, bytes, cudaMemcpyHostToDevice, h->st));
+    /* copy stream: wait until the kernels of two blocks ago are done with raw[i]; the kernel
+     * stream waits for the copy, so the copy overlaps the previous block's kernels */
+    TXG_CUDA_TRY(cudaStreamWaitEvent(h->cst, h->raw_free[i], 0));
+    TXG_CUDA_TRY(cudaMemcpyAsync(h->raw[i], src, bytes, cudaMemcpyHostToDevice, h->cst));
+    TXG_CUDA_TRY(cudaEventRecord(h->raw_loaded[i], h->cst));
+    TXG_CUDA_TRY(cudaStreamWaitEvent(h->st, h->raw_loaded[i], 0));
     int rc = run_block(h, beam, h->raw[i]);
     TXG_CUDA_TRY(cudaEventRecord(h->raw_free[i], h->st));
     return rc;
@@ -622,6 +806,7 @@ int txg_sync(txg_handle *h)
                 if (rc && (status == TXG_OK || status == TXG_ERR_OVERFLOW)) status = rc;
             }
         }
+    h->pool->drain();
     return status;
 }
 
@@ -643,11 +828,13 @@ int txg_get_candidates(txg_handle *h, int32_t beam, int32_t row, txg_cand *out, 
     if (rc) return rc;
     const BeamRow &b = h->br[beam][row];
     if (n) *n = b.last_count;
+    if (!b.last) return TXG_OK;
+    h->pool->wait(*b.last);
     if (out && cap > 0) {
-        long m = std::min<long>(cap, (long)b.last.size());
-        if (m > 0) memcpy(out, b.last.data(), m * sizeof(txg_cand));
+        long m = std::min<long>(cap, (long)b.last->cands.size());
+        if (m > 0) memcpy(out, b.last->cands.data(), m * sizeof(txg_cand));
     }
-    return b.last_count > h->cap ? TXG_ERR_OVERFLOW : TXG_OK;
+    return result_status(h, *b.last);
 }
 
 int txg_pop_result(txg_handle *h, int32_t beam, int32_t row, txg_result *res, txg_cand *points,
@@ -657,7 +844,10 @@ int txg_pop_result(txg_handle *h, int32_t beam, int32_t row, txg_result *res, tx
     if (rc) return rc;
     BeamRow &b = h->br[beam][row];
     if (b.fifo.empty()) return fail(TXG_ERR_STATE, "no block result waiting");
-    Result &r = b.fifo.front();
+    ResultP rp = b.fifo.front();
+    b.fifo.pop_front();
+    h->pool->wait(*rp);
+    const Result &r = *rp;
     const bool over = r.count > h->cap;
     if (res) {
         res->counter = r.counter;
@@ -674,8 +864,7 @@ int txg_pop_result(txg_handle *h, int32_t beam, int32_t row, txg_result *res, tx
         const long m = std::min<long>(ccap, (long)r.clusters.size());
         if (m > 0) memcpy(clusters, r.clusters.data(), m * sizeof(txg_cand));
     }
-    b.fifo.pop_front();
-    return over ? TXG_ERR_OVERFLOW : TXG_OK;
+    return result_status(h, r);
 }
 
 int txg_get_dense(txg_handle *h, int32_t beam, int32_t row, float *mxS, int32_t *mxwn)
