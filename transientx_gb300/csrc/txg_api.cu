@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <condition_variable>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <functional>
@@ -165,6 +166,7 @@ struct Workers {
 
 struct BeamRow {
     float *xh[2] = {nullptr, nullptr};
+    __half *x16 = nullptr; /* FP16 copy of the current buffer (16-bit precisions) */
     int cur = 0;
     float *ds = nullptr;
     int32_t *ranges[8] = {nullptr};
@@ -477,15 +479,17 @@ int run_block(txg_handle *h, int beam, const uint8_t *raw)
             else if (P.cfg.rfi_kind[q] == TXG_RFI_ZDOT)
                 launch_zdot(x, P.ldh, P.C, P.N, b.s, b.sst, h->st);
         }
+        /* 16-bit precisions: stage 1 reads an FP16 copy (history columns included) */
+        if (b.x16) launch_to_half(xcur, P.ldh, P.C, P.H + P.N, b.x16, h->st);
         if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[2], h->st));
 
         /* stage 1: new subband samples t in [counter-N-maxd1, counter-maxd1) */
         const long counter = b.pushed + P.N;
         const long tbase = counter - P.N - P.maxd1;
         TXG_CUDA_TRY(cudaMemsetAsync(sl.dcount, 0, 2 * sizeof(int), h->st));
-        launch_stage1(xcur, P.ldh, P.H - P.maxd1, P.C, P.N, P.nsub, P.ng, D.sub_start, D.d1,
-                      P.maxd1, P.maxch, b.ring, P.R, pmod(tbase, P.R), h->prec, sl.dcount + 1,
-                      h->st);
+        launch_stage1(xcur, b.x16, P.ldh, P.H - P.maxd1, P.C, P.N, P.nsub, P.ng, D.sub_start, D.d1,
+                      P.maxd1, P.maxch, b.ring, P.R, pmod(tbase, P.R), h->prec, P.s1_var,
+                      sl.dcount + 1, h->st);
         TXG_CUDA_TRY(cudaGetLastError());
         if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[3], h->st));
 
@@ -493,7 +497,7 @@ int run_block(txg_handle *h, int beam, const uint8_t *raw)
         if (gated) {
             const long t0 = counter - P.N - P.offset;
             launch_stage2(b.ring, P.R, P.nsub, P.G, P.cfg.ndm, P.nout, D.d2, P.s2_span,
-                          pmod(t0, P.R), h->prec, b.tim, P.nout, sl.dcount + 1, h->st);
+                          pmod(t0, P.R), h->prec, P.s2_kb, b.tim, P.nout, sl.dcount + 1, h->st);
             TXG_CUDA_TRY(cudaGetLastError());
             if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[4], h->st));
             rc = launch_boxcar(b.tim, P.nout, P.cfg.ndm, P.nout, D.vwn, (int)P.vwn.size(),
@@ -535,10 +539,16 @@ int finish_plan(RowPlan &P, int r)
     if (P.R < need) P.R = (need + 31) / 32 * 32;
     P.maxch = 0;
     for (int s = 0; s < P.nsub; s++) P.maxch = std::max(P.maxch, P.sub_start[s + 1] - P.sub_start[s]);
-    /* a stage-1 tile copy starts at most 3 columns before its tile and spans the 512-sample
-     * tile plus the largest within-subband delay plus alignment, so it may read up to
-     * H + N + 517 columns: pad the pitch past that */
-    P.ldh = ((P.H + P.N + 544) + 31) / 32 * 32;
+    /* a stage-1 tile copy starts at most 7 columns before its tile and spans the tile (at
+     * most 1024 samples) plus the largest within-subband delay plus alignment and one pair
+     * element, so it may read up to H + N + 1040 columns: pad the pitch past that */
+    P.ldh = ((P.H + P.N + 1056) + 31) / 32 * 32;
+    /* launch shapes; TXG_DEDISP_SHAPE="s1=<variant>,s2kb=<KB>" overrides them */
+    if (const char *e = getenv("TXG_DEDISP_SHAPE")) {
+        int v = 0;
+        if (const char *q = strstr(e, "s1=")) P.s1_var = (sscanf(q + 3, "%d", &v) == 1) ? v : P.s1_var;
+        if (const char *q = strstr(e, "s2kb=")) P.s2_kb = (sscanf(q + 5, "%d", &v) == 1 && v >= 16 && v <= 200) ? v : P.s2_kb;
+    }
     if ((size_t)P.nout > boxcar_max_samples())
         return fail(TXG_ERR_UNSUPPORTED, "row " + std::to_string(r) +
                                              ": ndump+noverlap exceeds the boxcar row limit of " +
@@ -699,6 +709,7 @@ int txg_create(const txg_plan *plan, txg_handle **out)
             BeamRow &b = h->br[beam][r];
             for (int i = 0; i < 2; i++)
                 if ((rc = dalloc(h, &b.xh[i], (size_t)P.C * P.ldh))) return bail(rc);
+            if (h->prec != TXG_PREC_FP32 && (rc = dalloc(h, &b.x16, (size_t)P.C * P.ldh))) return bail(rc);
             long kmax = 1;
             for (int q = 0; q < P.cfg.nrfi; q++)
                 if (P.cfg.rfi_kind[q] == TXG_RFI_KADANEF) {

@@ -15,6 +15,9 @@
  * input element crosses HBM/L2 once per CTA tile.  A wait that runs out sets *err and the
  * CTA returns without touching its outputs.
  */
+#include <algorithm>
+#include <type_traits>
+
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -191,28 +194,27 @@ k_stage1(const float *__restrict__ xh, long ldh, long col0, int C, long N, int n
 }
 
 /* Stage 1 with the subband's whole channel window resident in shared memory: one CTA per
- * (512-sample tile, subband) loads every channel row of the subband once (so each input
- * element crosses HBM once per tile) and then walks all coarse-DM groups, 16 at a time.  Each
- * output adds its channels in ascending order from 0.0f. */
-constexpr int S1R_THREADS = 256;
-constexpr int S1R_U = 2;
-constexpr int S1R_TT = S1R_THREADS * S1R_U;
-
-template <typename T>
-__global__ void __launch_bounds__(S1R_THREADS)
+ * (TH*U-sample tile, subband) loads every channel row of the subband once (so each input
+ * element crosses HBM once per tile) and then walks all coarse-DM groups, GS*GPT at a time:
+ * the CTA's GS thread sets share the window and take GPT groups each.  Each output adds its
+ * channels in ascending order from 0.0f. */
+template <typename T, int TH, int U, int GS, int GPT>
+__global__ void __launch_bounds__(TH * GS)
 k_stage1r(const float *__restrict__ xh, long ldh, long col0, int C, long N, int nsub, int ng,
           const int32_t *__restrict__ sub_start, const int32_t *__restrict__ d1, long wmax,
           int maxch, T *__restrict__ ring, long R, long tbase_mod, int *err)
 {
+    constexpr int NT = TH * GS, TT = TH * U, GPC = GS * GPT;
+    static_assert(GPT % 4 == 0, "delays are read four at a time");
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ __align__(8) uint64_t bar;
     __shared__ int span_sh;
     float *win = reinterpret_cast<float *>(smraw);
     int32_t *dsm = reinterpret_cast<int32_t *>(win + (size_t)maxch * wmax);
     const int s = blockIdx.y;
-    const long u0 = (long)blockIdx.x * S1R_TT;
+    const long u0 = (long)blockIdx.x * TT;
     const int j0 = sub_start[s], j1 = sub_start[s + 1], jn = j1 - j0;
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lt = tid % TH, gs = tid / TH;
     const long cstart = (u0 + col0) & ~3L;
     const int al = (int)(u0 + col0 - cstart);
 
@@ -222,10 +224,9 @@ k_stage1r(const float *__restrict__ xh, long ldh, long col0, int C, long N, int 
         span_sh = 0;
     }
     __syncthreads();
-    for (int jj = tid; jj < jn; jj += S1R_THREADS)
-        atomicMax(&span_sh, d1[(size_t)(ng - 1) * C + j0 + jj]);
+    for (int jj = tid; jj < jn; jj += NT) atomicMax(&span_sh, d1[(size_t)(ng - 1) * C + j0 + jj]);
     __syncthreads();
-    const long W = ((long)S1R_TT + span_sh + al + 3) / 4 * 4; /* <= wmax */
+    const long W = ((long)TT + span_sh + al + 3) / 4 * 4; /* <= wmax */
     if (tid == 0) {
         const uint32_t bytes = (uint32_t)(W * sizeof(float));
         mbar_expect_tx(&bar, bytes * (uint32_t)jn);
@@ -238,51 +239,44 @@ k_stage1r(const float *__restrict__ xh, long ldh, long col0, int C, long N, int 
         mbar_wait(&bar, 0);
         return;
     }
-    for (int g0 = 0; g0 < ng; g0 += S1_GPC) {
-        const int gn = min(S1_GPC, ng - g0);
+    for (int g0 = 0; g0 < ng; g0 += GPC) {
+        const int gn = min(GPC, ng - g0);
         /* delays of the chunk; groups past the end repeat the last one (no reload) */
-        for (int e = tid; e < jn * S1_GPC; e += S1R_THREADS) {
-            const int jj = e / S1_GPC, g = e % S1_GPC;
+        for (int e = tid; e < jn * GPC; e += NT) {
+            const int jj = e / GPC, g = e % GPC;
             dsm[e] = d1[(size_t)(g0 + (g < gn ? g : gn - 1)) * C + j0 + jj];
         }
         __syncthreads();
-        float acc[S1_GPC][S1R_U];
+        float acc[GPT][U];
 #pragma unroll
-        for (int g = 0; g < S1_GPC; g++)
+        for (int g = 0; g < GPT; g++)
 #pragma unroll
-            for (int q = 0; q < S1R_U; q++) acc[g][q] = 0.f;
+            for (int q = 0; q < U; q++) acc[g][q] = 0.f;
         for (int jj = 0; jj < jn; jj++) {
-            const float *wr = win + (size_t)jj * W + al + tid;
-            const int4 *dv = reinterpret_cast<const int4 *>(dsm + jj * S1_GPC);
-            int dd[S1_GPC];
+            const float *wr = win + (size_t)jj * W + al + lt;
+            const int4 *dv = reinterpret_cast<const int4 *>(dsm + jj * GPC + gs * GPT);
+            int dd[GPT];
 #pragma unroll
-            for (int gq = 0; gq < S1_GPC / 4; gq++) {
+            for (int gq = 0; gq < GPT / 4; gq++) {
                 const int4 d = dv[gq];
                 dd[4 * gq] = d.x;
                 dd[4 * gq + 1] = d.y;
                 dd[4 * gq + 2] = d.z;
                 dd[4 * gq + 3] = d.w;
             }
-            float v[S1R_U];
 #pragma unroll
-            for (int q = 0; q < S1R_U; q++) v[q] = wr[dd[0] + q * S1R_THREADS];
+            for (int g = 0; g < GPT; g++)
 #pragma unroll
-            for (int g = 0; g < S1_GPC; g++) {
-                if (g > 0) {
-#pragma unroll
-                    for (int q = 0; q < S1R_U; q++) v[q] = wr[dd[g] + q * S1R_THREADS];
-                }
-#pragma unroll
-                for (int q = 0; q < S1R_U; q++) acc[g][q] = __fadd_rn(acc[g][q], v[q]);
-            }
+                for (int q = 0; q < U; q++) acc[g][q] = __fadd_rn(acc[g][q], wr[dd[g] + q * TH]);
         }
 #pragma unroll
-        for (int g = 0; g < S1_GPC; g++) {
-            if (g < gn) {
-                T *out = ring + ((size_t)(g0 + g) * nsub + s) * R;
+        for (int g = 0; g < GPT; g++) {
+            const int gc = gs * GPT + g;
+            if (gc < gn) {
+                T *out = ring + ((size_t)(g0 + gc) * nsub + s) * R;
 #pragma unroll
-                for (int q = 0; q < S1R_U; q++) {
-                    const long u = u0 + tid + q * S1R_THREADS;
+                for (int q = 0; q < U; q++) {
+                    const long u = u0 + lt + q * TH;
                     if (u < N) {
                         long t = tbase_mod + u;
                         t = t >= R ? t - R : t;
@@ -292,6 +286,148 @@ k_stage1r(const float *__restrict__ xh, long ldh, long col0, int C, long N, int 
             }
         }
         __syncthreads();
+    }
+}
+
+/* ---- 16-bit pairs ---------------------------------------------------------------------- */
+/* FP32 += one 16-bit value (exact conversion, one rounding), PTX mixed-precision add. */
+__device__ __forceinline__ void addp(float &lo_acc, float &hi_acc, uint32_t v, __half)
+{
+    asm("{ .reg .b16 l, h; mov.b32 {l, h}, %2; add.rn.f32.f16 %0, l, %0; add.rn.f32.f16 %1, h, %1; }"
+        : "+f"(lo_acc), "+f"(hi_acc)
+        : "r"(v));
+}
+__device__ __forceinline__ void addp(float &lo_acc, float &hi_acc, uint32_t v, __nv_bfloat16)
+{
+    asm("{ .reg .b16 l, h; mov.b32 {l, h}, %2; add.rn.f32.bf16 %0, l, %0; add.rn.f32.bf16 %1, h, %1; }"
+        : "+f"(lo_acc), "+f"(hi_acc)
+        : "r"(v));
+}
+
+/* Odd-aligned pair copy of a 16-bit window: o[k] = (e[2k+1], e[2k+2]) as one word. */
+__device__ __forceinline__ void build_odd(const uint32_t *e, uint32_t *o, long nwords, int tid, int nth)
+{
+    for (long k = tid; k < nwords; k += nth) o[k] = __byte_perm(e[k], e[k + 1], 0x5432);
+}
+
+/* Stage 1 on the FP16 copy of the block, two consecutive samples per 32-bit shared-memory
+ * load.  Each channel window is held twice, as even-aligned pairs (the bulk copy) and as
+ * odd-aligned pairs (built in shared memory), so a sample pair at any delay is one aligned
+ * word.  GS thread sets share the window and take GPT coarse-DM groups each.  Sums are FP32
+ * in ascending channel order; the ring stores T. */
+template <typename T, int TH, int UP, int GS, int GPT>
+__global__ void __launch_bounds__(TH * GS)
+k_stage1p(const __half *__restrict__ xh, long ldh, long col0, int C, long N, int nsub, int ng,
+          const int32_t *__restrict__ sub_start, const int32_t *__restrict__ d1, long wmax,
+          int maxch, T *__restrict__ ring, long R, long tbase_mod, int *err)
+{
+    constexpr int NT = TH * GS, TT = 2 * TH * UP, GPC = GS * GPT;
+    static_assert(GPT % 4 == 0, "delays are read four at a time");
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ int span_sh;
+    uint32_t *words = reinterpret_cast<uint32_t *>(smraw);
+    const int s = blockIdx.y;
+    const long u0 = (long)blockIdx.x * TT;
+    const int j0 = sub_start[s], j1 = sub_start[s + 1], jn = j1 - j0;
+    const int tid = threadIdx.x, lt = tid % TH, gs = tid / TH;
+    const long cstart = (u0 + col0) & ~7L; /* 16-byte boundary */
+    const int al = (int)(u0 + col0 - cstart);
+
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+        span_sh = 0;
+    }
+    __syncthreads();
+    for (int jj = tid; jj < jn; jj += NT) atomicMax(&span_sh, d1[(size_t)(ng - 1) * C + j0 + jj]);
+    __syncthreads();
+    /* halves per window: the pair at the largest delay ends inside it */
+    const long W = ((long)TT + span_sh + al + 2 + 7) / 8 * 8; /* <= wmax */
+    const long ES = (W + 8) / 2;                             /* even-pair words per channel */
+    const long OS = W / 2;                                   /* odd-pair words per channel */
+    uint32_t *ew = words, *ow = words + (size_t)jn * ES;
+    int32_t *dsm = reinterpret_cast<int32_t *>(ow + (size_t)jn * OS);
+    if (tid == 0) {
+        const uint32_t bytes = (uint32_t)(W * sizeof(__half));
+        mbar_expect_tx(&bar, bytes * (uint32_t)jn);
+        for (int jj = 0; jj < jn; jj++)
+            bulk_g2s(ew + (size_t)jj * ES, xh + (long)(j0 + jj) * ldh + cstart, bytes, &bar);
+    }
+    const bool ok = mbar_wait(&bar, 0);
+    if (!__syncthreads_and(ok)) {
+        if (tid == 0) atomicExch(err, 1);
+        mbar_wait(&bar, 0);
+        return;
+    }
+    for (int jj = 0; jj < jn; jj++) build_odd(ew + (size_t)jj * ES, ow + (size_t)jj * OS, OS, tid, NT);
+    for (int g0 = 0; g0 < ng; g0 += GPC) {
+        const int gn = min(GPC, ng - g0);
+        /* word offset of the pair at (channel, delay): even or odd copy by the parity */
+        for (int e = tid; e < jn * GPC; e += NT) {
+            const int jj = e / GPC, g = e % GPC;
+            const int h = al + d1[(size_t)(g0 + (g < gn ? g : gn - 1)) * C + j0 + jj];
+            dsm[e] = (h & 1) ? (int)((size_t)jn * ES + (size_t)jj * OS + (h - 1) / 2)
+                             : (int)((size_t)jj * ES + h / 2);
+        }
+        __syncthreads();
+        float acc[GPT][2 * UP];
+#pragma unroll
+        for (int g = 0; g < GPT; g++)
+#pragma unroll
+            for (int q = 0; q < 2 * UP; q++) acc[g][q] = 0.f;
+        const uint32_t *wr = words + lt;
+        for (int jj = 0; jj < jn; jj++) {
+            const int4 *dv = reinterpret_cast<const int4 *>(dsm + jj * GPC + gs * GPT);
+            int dd[GPT];
+#pragma unroll
+            for (int gq = 0; gq < GPT / 4; gq++) {
+                const int4 d = dv[gq];
+                dd[4 * gq] = d.x;
+                dd[4 * gq + 1] = d.y;
+                dd[4 * gq + 2] = d.z;
+                dd[4 * gq + 3] = d.w;
+            }
+#pragma unroll
+            for (int g = 0; g < GPT; g++)
+#pragma unroll
+                for (int q = 0; q < UP; q++)
+                    addp(acc[g][2 * q], acc[g][2 * q + 1], wr[dd[g] + q * TH], __half());
+        }
+#pragma unroll
+        for (int g = 0; g < GPT; g++) {
+            const int gc = gs * GPT + g;
+            if (gc < gn) {
+                T *out = ring + ((size_t)(g0 + gc) * nsub + s) * R;
+#pragma unroll
+                for (int q = 0; q < 2 * UP; q++) {
+                    const long u = u0 + 2 * (lt + (q >> 1) * TH) + (q & 1);
+                    if (u < N) {
+                        long t = tbase_mod + u;
+                        t = t >= R ? t - R : t;
+                        out[t] = to_store<T>(acc[g][q]);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+/* FP16 copy of columns [0, ncols) of the channel buffer, values clamped to the FP16 range. */
+__global__ void k_to_half(const float *__restrict__ x, long ldh, int C, long ncols4,
+                          __half *__restrict__ y)
+{
+    const long total = (long)C * ncols4;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const long j = i / ncols4, c4 = i - j * ncols4;
+        const float4 v = *reinterpret_cast<const float4 *>(x + j * ldh + 4 * c4);
+        const float lim = 65504.f;
+        __half2 a = __floats2half2_rn(fminf(fmaxf(v.x, -lim), lim), fminf(fmaxf(v.y, -lim), lim));
+        __half2 b = __floats2half2_rn(fminf(fmaxf(v.z, -lim), lim), fminf(fmaxf(v.w, -lim), lim));
+        __half2 *o = reinterpret_cast<__half2 *>(y + j * ldh + 4 * c4);
+        o[0] = a;
+        o[1] = b;
     }
 }
 
@@ -433,9 +569,142 @@ k_stage2(const T *__restrict__ ring, long R, int nsub, int G, long ndm, long nou
     }
 }
 
+/* Stage 2 on a 16-bit ring, two consecutive samples per 32-bit shared-memory load: the
+ * subband windows are held as even-aligned pairs (bulk copies) and odd-aligned pairs (built
+ * in shared memory).  Same order of additions as k_stage2. */
+template <typename T, int KPC, int TH>
+__global__ void __launch_bounds__(TH)
+k_stage2p(const T *__restrict__ ring, long R, int nsub, int G, long ndm, long nout,
+          const int32_t *__restrict__ d2, long t0_mod, int sc, long wtot_max,
+          float *__restrict__ tim, long ldt, int *err)
+{
+    constexpr int TT = 2 * TH;
+    constexpr int EPC = 8; /* 16-bit elements per 16 bytes */
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ __align__(8) uint64_t bar;
+    uint32_t *words = reinterpret_cast<uint32_t *>(smraw);
+    T *win = reinterpret_cast<T *>(smraw);
+    /* even pairs: wtot_max halves + one pad word; odd pairs: wtot_max/2 words */
+    const long ewords = wtot_max / 2 + 4;
+    uint32_t *ow = words + ewords;
+    int32_t *doff = reinterpret_cast<int32_t *>(ow + wtot_max / 2);
+    int32_t *wts = doff + sc * KPC, *wal = wts + sc, *wlen = wal + sc, *wpos = wlen + sc;
+    const int tid = threadIdx.x;
+    const int nkc = (G + KPC - 1) / KPC;
+    const int g = blockIdx.y / nkc, kc = blockIdx.y % nkc;
+    const long k0 = (long)g * G + (long)kc * KPC;
+    const long kend = min((long)(g + 1) * G, ndm);
+    const int kn = (int)min((long)KPC, kend - k0);
+    if (kn <= 0) return;
+    const long u0 = (long)blockIdx.x * TT;
+
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+
+    float acc[KPC][2];
+#pragma unroll
+    for (int k = 0; k < KPC; k++) acc[k][0] = acc[k][1] = 0.f;
+
+    uint32_t phase = 0;
+    for (int s0 = 0; s0 < nsub; s0 += sc) {
+        const int sn = min(sc, nsub - s0);
+        /* windows: ring start rounded down to 16 bytes, length covering the last pair */
+        for (int ss = tid; ss < sn; ss += TH) {
+            const int s = s0 + ss;
+            const long lo = d2[(size_t)k0 * nsub + s];
+            const long hi = d2[(size_t)(k0 + kn - 1) * nsub + s];
+            long tstart = (t0_mod + u0 + lo) % R;
+            const long al = tstart % EPC;
+            tstart -= al;
+            wts[ss] = (int32_t)tstart;
+            wal[ss] = (int32_t)al;
+            wlen[ss] = (int32_t)(((long)TT + (hi - lo) + al + 2 + EPC - 1) / EPC * EPC);
+        }
+        __syncthreads();
+        if (tid < 32) { /* exclusive prefix of the lengths (one warp) */
+            int carry = 0;
+            for (int base = 0; base < sn; base += 32) {
+                const int ss = base + tid;
+                const int v = ss < sn ? wlen[ss] : 0;
+                int incl = v;
+#pragma unroll
+                for (int off = 1; off < 32; off <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, incl, off);
+                    if (tid >= off) incl += y;
+                }
+                if (ss < sn) wpos[ss] = carry + incl - v;
+                carry += __shfl_sync(0xffffffffu, incl, 31);
+            }
+            if (tid == 0) {
+                fence_proxy_async();
+                mbar_expect_tx(&bar, (uint32_t)(carry * (int)sizeof(T)));
+            }
+        }
+        __syncthreads();
+        /* word offsets of each (subband, DM): even or odd copy by the parity */
+        for (int e = tid; e < sn * KPC; e += TH) {
+            const int ss = e / KPC, k = e % KPC;
+            const int lo = d2[(size_t)k0 * nsub + s0 + ss];
+            const int h = wpos[ss] + wal[ss] + d2[(size_t)(k0 + (k < kn ? k : kn - 1)) * nsub + s0 + ss] - lo;
+            doff[e] = (h & 1) ? (int)(ewords + (h - 1) / 2) : h / 2;
+        }
+        for (int ss = tid; ss < sn; ss += TH) {
+            const T *row = ring + ((size_t)g * nsub + s0 + ss) * R;
+            const long pos = wpos[ss], len = wlen[ss], tstart = wts[ss];
+            const long first = min(len, R - tstart);
+            fence_proxy_async();
+            bulk_g2s(win + pos, row + tstart, (uint32_t)(first * sizeof(T)), &bar);
+            if (first < len)
+                bulk_g2s(win + pos + first, row, (uint32_t)((len - first) * sizeof(T)), &bar);
+        }
+        __syncthreads();
+        bool ok = mbar_wait(&bar, phase);
+        phase ^= 1;
+        if (!__syncthreads_and(ok)) {
+            if (tid == 0) atomicExch(err, 2);
+            mbar_wait(&bar, phase ^ 1);
+            return;
+        }
+        {
+            const long nw = (wpos[sn - 1] + wlen[sn - 1]) / 2;
+            build_odd(words, ow, nw, tid, TH);
+        }
+        __syncthreads();
+        const uint32_t *wr = words + tid;
+        for (int ss = 0; ss < sn; ss++) {
+            const int4 *dv = reinterpret_cast<const int4 *>(doff + ss * KPC);
+            int dd[KPC];
+#pragma unroll
+            for (int kq = 0; kq < KPC / 4; kq++) {
+                const int4 d = dv[kq];
+                dd[4 * kq] = d.x;
+                dd[4 * kq + 1] = d.y;
+                dd[4 * kq + 2] = d.z;
+                dd[4 * kq + 3] = d.w;
+            }
+#pragma unroll
+            for (int k = 0; k < KPC; k++) addp(acc[k][0], acc[k][1], wr[dd[k]], T());
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int k = 0; k < KPC; k++) {
+        if (k < kn) {
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                const long u = u0 + 2 * tid + q;
+                if (u < nout) tim[(k0 + k) * ldt + u] = acc[k][q];
+            }
+        }
+    }
+}
+
 inline unsigned nblk(long n, int b) { return (unsigned)((n + b - 1) / b); }
 
-constexpr size_t SMEM_BUDGET = 100 * 1024;     /* two CTAs per SM overlap copies and math */
+constexpr size_t SMEM_BUDGET = 100 * 1024;     /* chunked stage 1: two CTAs per SM */
 constexpr size_t RESIDENT_BUDGET = 200 * 1024; /* whole-subband stage-1 windows */
 
 } // namespace
@@ -443,29 +712,46 @@ constexpr size_t RESIDENT_BUDGET = 200 * 1024; /* whole-subband stage-1 windows 
 /* Largest window any stage-1 CTA needs: tile + maxd1 + alignment (delays grow with the
  * group index).  xh points at column 0 of the channel buffer; col0 = H - maxd1.  When the
  * widest subband's full window fits in shared memory the resident kernel reads every channel
- * row once; otherwise the chunked kernel (channel chunks, 16 groups per CTA) is used. */
-void launch_stage1(const float *xh, long ldh, long col0, int C, long N, int nsub, int ng,
-                   const int32_t *sub_start, const int32_t *d1, long maxd1, int maxch, void *ring,
-                   long R, long tbase_mod, int prec, int *err, cudaStream_t st)
+ * row once; otherwise the chunked kernel (channel chunks, 16 groups per CTA) is used.  The
+ * 16-bit precisions read the FP16 copy x16 with the pair kernel when its windows fit. */
+template <typename T, int TH, int U, int GS, int GPT>
+static bool stage1r_try(const float *xh, long ldh, long col0, int C, long N, int nsub, int ng,
+                        const int32_t *sub_start, const int32_t *d1, long maxd1, int maxch, T *ring,
+                        long R, long tbase_mod, int *err, cudaStream_t st)
 {
-    const long wr = ((long)S1R_TT + maxd1 + 3 + 3) / 4 * 4;
-    const size_t smem_r = (size_t)maxch * wr * sizeof(float) + (size_t)maxch * S1_GPC * sizeof(int32_t);
-    if (smem_r <= RESIDENT_BUDGET) {
-        dim3 grid(nblk(N, S1R_TT), nsub);
-#define TXG_S1R(TY)                                                                                \
-    cudaFuncSetAttribute(k_stage1r<TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r);  \
-    k_stage1r<TY><<<grid, S1R_THREADS, smem_r, st>>>(xh, ldh, col0, C, N, nsub, ng, sub_start, d1, \
-                                                     wr, maxch, (TY *)ring, R, tbase_mod, err)
-        if (prec == TXG_PREC_BF16) {
-            TXG_S1R(__nv_bfloat16);
-        } else if (prec == TXG_PREC_FP16) {
-            TXG_S1R(__half);
-        } else {
-            TXG_S1R(float);
-        }
-#undef TXG_S1R
-        return;
-    }
+    const long tt = (long)TH * U;
+    const long wr = (tt + maxd1 + 3 + 3) / 4 * 4;
+    const size_t smem = (size_t)maxch * wr * sizeof(float) + (size_t)maxch * GS * GPT * sizeof(int32_t);
+    if (smem > RESIDENT_BUDGET) return false;
+    auto kern = k_stage1r<T, TH, U, GS, GPT>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<dim3(nblk(N, (int)tt), nsub), TH * GS, smem, st>>>(xh, ldh, col0, C, N, nsub, ng, sub_start,
+                                                              d1, wr, maxch, ring, R, tbase_mod, err);
+    return true;
+}
+
+template <typename T, int TH, int UP, int GS, int GPT>
+static bool stage1p_try(const __half *x16, long ldh, long col0, int C, long N, int nsub, int ng,
+                        const int32_t *sub_start, const int32_t *d1, long maxd1, int maxch, T *ring,
+                        long R, long tbase_mod, int *err, cudaStream_t st)
+{
+    const long tt = 2L * TH * UP;
+    const long w = (tt + maxd1 + 7 + 2 + 7) / 8 * 8;
+    const size_t smem =
+        (size_t)maxch * ((w + 8) * 2 + w * 2) + (size_t)maxch * GS * GPT * sizeof(int32_t);
+    if (smem > RESIDENT_BUDGET) return false;
+    auto kern = k_stage1p<T, TH, UP, GS, GPT>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<dim3(nblk(N, (int)tt), nsub), TH * GS, smem, st>>>(x16, ldh, col0, C, N, nsub, ng, sub_start,
+                                                              d1, w, maxch, ring, R, tbase_mod, err);
+    return true;
+}
+
+template <typename T>
+static void stage1_chunked(const float *xh, long ldh, long col0, int C, long N, int nsub, int ng,
+                           const int32_t *sub_start, const int32_t *d1, long maxd1, int maxch,
+                           T *ring, long R, long tbase_mod, int *err, cudaStream_t st)
+{
     long wmax = ((long)S1_TT + maxd1 + 3 + 3) / 4 * 4;
     size_t per = wmax * sizeof(float) + S1_GPC * sizeof(int32_t);
     int cj = (int)((SMEM_BUDGET - 64) / per);
@@ -473,19 +759,79 @@ void launch_stage1(const float *xh, long ldh, long col0, int C, long N, int nsub
     if (cj < 1) cj = 1;
     size_t smem = (size_t)cj * wmax * sizeof(float) + (size_t)cj * S1_GPC * sizeof(int32_t);
     dim3 grid(nblk(N, S1_TT), nsub, nblk(ng, S1_GPC));
-    if (prec == TXG_PREC_BF16) {
-        cudaFuncSetAttribute(k_stage1<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_stage1<__nv_bfloat16><<<grid, S1_THREADS, smem, st>>>(
-            xh, ldh, col0, C, N, nsub, ng, sub_start, d1, cj, wmax, (__nv_bfloat16 *)ring, R, tbase_mod, err);
-    } else if (prec == TXG_PREC_FP16) {
-        cudaFuncSetAttribute(k_stage1<__half>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_stage1<__half><<<grid, S1_THREADS, smem, st>>>(
-            xh, ldh, col0, C, N, nsub, ng, sub_start, d1, cj, wmax, (__half *)ring, R, tbase_mod, err);
+    cudaFuncSetAttribute(k_stage1<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_stage1<T><<<grid, S1_THREADS, smem, st>>>(xh, ldh, col0, C, N, nsub, ng, sub_start, d1, cj,
+                                                wmax, ring, R, tbase_mod, err);
+}
+
+/* Resident launch shapes (threads per set x samples per thread, thread sets x groups each):
+ *   FP32 windows: 0 = 256x2 4x8 (default), 1 = 256x2 1x16, 2 = 512x1 1x16, 3 = 256x2 2x8,
+ *                 4 = 256x2 2x16, 5 = 256x1 2x8, 6 = 256x2 4x4
+ *   16-bit pairs: 0 = 256x1 4x8 (default), 1 = 256x1 1x16, 2 = 256x1 2x8, 3 = 256x1 2x16,
+ *                 4 = 256x1 4x4, 5 = 128x1 4x8, 6 = 128x2 4x8
+ * (measured on the 4096-channel workload: more warps per SM over the same resident window
+ * pay until the per-thread delay loads dominate).  A shape whose windows do not fit falls back
+ * to 1x16, then to the chunked kernel. */
+template <typename T>
+static void stage1_dispatch(const float *xh, const __half *x16, long ldh, long col0, int C, long N,
+                            int nsub, int ng, const int32_t *sub_start, const int32_t *d1, long maxd1,
+                            int maxch, T *ring, long R, long tbase_mod, int var, int *err,
+                            cudaStream_t st)
+{
+    bool done = false;
+#define TXG_ARGS xh, ldh, col0, C, N, nsub, ng, sub_start, d1, maxd1, maxch, ring, R, tbase_mod, err, st
+#define TXG_PARGS x16, ldh, col0, C, N, nsub, ng, sub_start, d1, maxd1, maxch, ring, R, tbase_mod, err, st
+    if constexpr (!std::is_same<T, float>::value) {
+        if (x16) {
+            switch (var) {
+            case 1: break;
+            case 2: done = stage1p_try<T, 256, 1, 2, 8>(TXG_PARGS); break;
+            case 3: done = stage1p_try<T, 256, 1, 2, 16>(TXG_PARGS); break;
+            case 4: done = stage1p_try<T, 256, 1, 4, 4>(TXG_PARGS); break;
+            case 5: done = stage1p_try<T, 128, 1, 4, 8>(TXG_PARGS); break;
+            case 6: done = stage1p_try<T, 128, 2, 4, 8>(TXG_PARGS); break;
+            default: done = stage1p_try<T, 256, 1, 4, 8>(TXG_PARGS); break;
+            }
+            if (!done) done = stage1p_try<T, 256, 1, 1, 16>(TXG_PARGS);
+        }
     } else {
-        cudaFuncSetAttribute(k_stage1<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_stage1<float><<<grid, S1_THREADS, smem, st>>>(
-            xh, ldh, col0, C, N, nsub, ng, sub_start, d1, cj, wmax, (float *)ring, R, tbase_mod, err);
+        switch (var) {
+        case 1: break;
+        case 2: done = stage1r_try<T, 512, 1, 1, 16>(TXG_ARGS); break;
+        case 3: done = stage1r_try<T, 256, 2, 2, 8>(TXG_ARGS); break;
+        case 4: done = stage1r_try<T, 256, 2, 2, 16>(TXG_ARGS); break;
+        case 5: done = stage1r_try<T, 256, 1, 2, 8>(TXG_ARGS); break;
+        case 6: done = stage1r_try<T, 256, 2, 4, 4>(TXG_ARGS); break;
+        default: done = stage1r_try<T, 256, 2, 4, 8>(TXG_ARGS); break;
+        }
     }
+    if (!done) done = stage1r_try<T, 256, 2, 1, 16>(TXG_ARGS);
+#undef TXG_ARGS
+#undef TXG_PARGS
+    if (!done) stage1_chunked<T>(xh, ldh, col0, C, N, nsub, ng, sub_start, d1, maxd1, maxch, ring, R, tbase_mod, err, st);
+}
+
+void launch_stage1(const float *xh, const __half *x16, long ldh, long col0, int C, long N, int nsub,
+                   int ng, const int32_t *sub_start, const int32_t *d1, long maxd1, int maxch, void *ring,
+                   long R, long tbase_mod, int prec, int var, int *err, cudaStream_t st)
+{
+    if (prec == TXG_PREC_BF16)
+        stage1_dispatch<__nv_bfloat16>(xh, x16, ldh, col0, C, N, nsub, ng, sub_start, d1, maxd1, maxch,
+                                       (__nv_bfloat16 *)ring, R, tbase_mod, var, err, st);
+    else if (prec == TXG_PREC_FP16)
+        stage1_dispatch<__half>(xh, x16, ldh, col0, C, N, nsub, ng, sub_start, d1, maxd1, maxch,
+                                (__half *)ring, R, tbase_mod, var, err, st);
+    else
+        stage1_dispatch<float>(xh, nullptr, ldh, col0, C, N, nsub, ng, sub_start, d1, maxd1, maxch,
+                               (float *)ring, R, tbase_mod, var, err, st);
+}
+
+void launch_to_half(const float *x, long ldh, int C, long ncols, __half *y, cudaStream_t st)
+{
+    const long n4 = (ncols + 3) / 4;
+    const long total = (long)C * n4;
+    const long blocks = std::min<long>((total + 255) / 256, 152L * 8);
+    k_to_half<<<(unsigned)blocks, 256, 0, st>>>(x, ldh, C, n4, y);
 }
 
 /* DMs per stage-2 CTA for a group of G fine DMs (one chunk per group when G <= 32). */
@@ -512,13 +858,13 @@ long stage2_window(long span) { return (long)S2_TT + span + 16; }
 
 template <typename T, int KPC>
 static void stage2_impl(const void *ring, long R, int nsub, int G, long ndm, long nout,
-                        const int32_t *d2, long span, long t0_mod, float *tim, long ldt, int *err,
-                        cudaStream_t st)
+                        const int32_t *d2, long span, long t0_mod, float *tim, long ldt, size_t budget,
+                        int *err, cudaStream_t st)
 {
     const long epc = 16 / (long)sizeof(T);
     const long wlen = ((long)S2_TT + span + 2 * epc) / epc * epc;
     const size_t per = wlen * sizeof(T) + KPC * sizeof(int32_t) + 5 * sizeof(int32_t);
-    int sc = (int)((SMEM_BUDGET - 64) / per);
+    int sc = (int)((budget - 64) / per);
     if (sc > nsub) sc = nsub;
     if (sc < 1) sc = 1;
     const long wtot = (long)sc * wlen;
@@ -531,29 +877,60 @@ static void stage2_impl(const void *ring, long R, int nsub, int G, long ndm, lon
                                                      t0_mod, sc, wtot, tim, ldt, err);
 }
 
-template <typename T>
+/* 16-bit ring: pair kernel, TT = 2 * 128 samples (the FP32 tile), windows doubled by the odd
+ * copy. */
+template <typename T, int KPC>
+static void stage2p_impl(const void *ring, long R, int nsub, int G, long ndm, long nout,
+                         const int32_t *d2, long span, long t0_mod, float *tim, long ldt, size_t budget,
+                         int *err, cudaStream_t st)
+{
+    constexpr int TH = S2_TT / 2;
+    const long wlen = ((long)S2_TT + span + 2 + 7 + 7) / 8 * 8; /* halves */
+    const size_t per = wlen * 4 + KPC * sizeof(int32_t) + 4 * sizeof(int32_t);
+    int sc = (int)((budget - 80) / per);
+    if (sc > nsub) sc = nsub;
+    if (sc < 1) sc = 1;
+    const long wtot = (long)sc * wlen;
+    const size_t smem = (size_t)(wtot / 2 + 4) * 4 + (size_t)(wtot / 2) * 4 + (size_t)sc * KPC * 4 +
+                        (size_t)sc * 4 * 4;
+    const int nkc = (G + KPC - 1) / KPC;
+    const long ng = (ndm + G - 1) / G;
+    dim3 grid(nblk(nout, S2_TT), (unsigned)(ng * nkc));
+    cudaFuncSetAttribute(k_stage2p<T, KPC, TH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_stage2p<T, KPC, TH><<<grid, TH, smem, st>>>((const T *)ring, R, nsub, G, ndm, nout, d2, t0_mod,
+                                                  sc, wtot, tim, ldt, err);
+}
+
+template <typename T, bool PAIRS>
 static void stage2_dispatch(const void *ring, long R, int nsub, int G, long ndm, long nout,
                             const int32_t *d2, long span, long t0_mod, float *tim, long ldt,
-                            int *err, cudaStream_t st)
+                            size_t budget, int *err, cudaStream_t st)
 {
+#define TXG_S2(K)                                                                                   \
+    if constexpr (PAIRS)                                                                            \
+        stage2p_impl<T, K>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, budget, err, st); \
+    else                                                                                            \
+        stage2_impl<T, K>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, budget, err, st)
     switch (stage2_kpc(G)) {
-    case 8: stage2_impl<T, 8>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, err, st); break;
-    case 16: stage2_impl<T, 16>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, err, st); break;
-    case 24: stage2_impl<T, 24>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, err, st); break;
-    default: stage2_impl<T, 32>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, err, st); break;
+    case 8: TXG_S2(8); break;
+    case 16: TXG_S2(16); break;
+    case 24: TXG_S2(24); break;
+    default: TXG_S2(32); break;
     }
+#undef TXG_S2
 }
 
 void launch_stage2(const void *ring, long R, int nsub, int G, long ndm, long nout,
-                   const int32_t *d2, long span, long t0_mod, int prec, float *tim, long ldt,
-                   int *err, cudaStream_t st)
+                   const int32_t *d2, long span, long t0_mod, int prec, int s2_kb, float *tim,
+                   long ldt, int *err, cudaStream_t st)
 {
+    const size_t budget = (size_t)(s2_kb >= 16 ? s2_kb : 36) * 1024;
     if (prec == TXG_PREC_BF16)
-        stage2_dispatch<__nv_bfloat16>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, err, st);
+        stage2_dispatch<__nv_bfloat16, true>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, budget, err, st);
     else if (prec == TXG_PREC_FP16)
-        stage2_dispatch<__half>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, err, st);
+        stage2_dispatch<__half, true>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, budget, err, st);
     else
-        stage2_dispatch<float>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, err, st);
+        stage2_dispatch<float, false>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, budget, err, st);
 }
 
 } // namespace txg

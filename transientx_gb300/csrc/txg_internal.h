@@ -9,6 +9,7 @@
 #include <string>
 #include <vector>
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "../../include/transientx_gb300.h"
@@ -41,6 +42,9 @@ struct RowPlan {
     std::vector<int32_t> zap_chan;
     long kad_wnlimit[8] = {0};
     float kad_thr = 0.f;
+    /* dedispersion launch shapes */
+    int s1_var = 0;   /* resident stage-1 launch shape, 0 = default */
+    int s2_kb = 36;   /* stage-2 shared memory per CTA, KB (36: six CTAs per SM) */
 };
 
 /* Deterministic planning helpers (txg_plan.cpp). */
@@ -75,14 +79,19 @@ void launch_kadane(float *x, long ldx, int C, long N, int tdk, int fdk, float th
                    long wnlimit, float *ds, int32_t *ranges, cudaStream_t st);
 void launch_zdot(float *x, long ldx, int C, long N, float *s, double *sstats,
                  cudaStream_t st);
-void launch_stage1(const float *xh, long ldh, long col0, int C, long N, int nsub, int ng,
-                   const int32_t *sub_start, const int32_t *d1, long maxd1, int maxch,
-                   void *ring, long R, long tbase_mod, int prec, int *err, cudaStream_t st);
+/* x16: FP16 copy of the channel buffer (same layout, used by the 16-bit precisions, may be
+ * null); var: resident launch shape (0 = default; see txg_dedisp.cu). */
+void launch_stage1(const float *xh, const __half *x16, long ldh, long col0, int C, long N, int nsub,
+                   int ng, const int32_t *sub_start, const int32_t *d1, long maxd1, int maxch,
+                   void *ring, long R, long tbase_mod, int prec, int var, int *err, cudaStream_t st);
+/* FP16 copy (values clamped to +-65504) of columns [0, ncols) of a [C][ldh] buffer */
+void launch_to_half(const float *x, long ldh, int C, long ncols, __half *y, cudaStream_t st);
 long stage2_span(const int32_t *d2h, int nsub, int G, long ndm);
 long stage2_window(long span);
+/* s2_kb: shared-memory budget of one stage-2 CTA in KB (CTAs per SM follow from it) */
 void launch_stage2(const void *ring, long R, int nsub, int G, long ndm, long nout,
-                   const int32_t *d2, long span, long t0_mod, int prec, float *tim, long ldt,
-                   int *err, cudaStream_t st);
+                   const int32_t *d2, long span, long t0_mod, int prec, int s2_kb, float *tim,
+                   long ldt, int *err, cudaStream_t st);
 int launch_boxcar(const float *tim, long ldt, long ndm, long n, const int32_t *vwn, int nw,
                   int iqr, int avx2_tail, float thre, txg_cand *cand, int *ncand, long cap,
                   float *mxS, int32_t *mxwn, int *err, cudaStream_t st);
