@@ -26,6 +26,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 ELEM = {"fp32": 4, "bf16": 2, "fp16": 2}
+# DRAM read+write bytes per launch of the dominant class from one ncu capture of this workload
+# (profiles/traffic_nchan4096_n2M_rfi_dm3000.md: mean over the three ddplan rows' launches)
+PROFILED_TRAFFIC = {("nchan4096_n2M_rfi_dm3000", "fp32", "stage1"): 1270.6e6,
+                    ("nchan4096_n2M_rfi_dm3000", "fp16", "stage1"): 608.4e6}
 ZAPTHRE = 4.0  # PreprocessLite skewness/kurtosis channel-zap threshold (transientx_fil default)
 
 
@@ -100,13 +104,16 @@ def measured_peaks():
 # ---- algorithmic bytes per kernel class (per launch, per row) ----------------------------
 def class_bytes(info, sp, nchans_raw, ndump_raw, ncand, elem):
     """Bytes a perfect implementation must move for one launch of each class:
-    unpack: raw uint8 in + float block out; preprocess: read+write the block once;
-    stage 1: block in + subband series out; stage 2: subband series in + dedispersed out;
-    boxcar: dedispersed series in + 16-byte candidates out."""
+    unpack: raw uint8 in + float block out; preprocess: read+write the block once (16-bit
+    precisions: plus its FP16 copy out); stage 1: block in (FP32, or its FP16 copy) + subband
+    series out; stage 2: subband series in + dedispersed out; boxcar: dedispersed series in +
+    16-byte candidates out."""
     C, N = info.nchans, info.ndump
     block = 4.0 * C * N
+    block_in = float(elem) * C * N
     series = float(elem) * info.nsub * info.ngroup * N
-    return [nchans_raw * ndump_raw + block, 2 * block, block + series,
+    pre = 2 * block + (block_in if elem == 2 else 0.0)
+    return [nchans_raw * ndump_raw + block, pre, block_in + series,
             series + 4.0 * info.ndm * info.nsamples, 4.0 * info.ndm * info.nsamples + 16 * ncand]
 
 
@@ -120,7 +127,7 @@ def launches_per_block(sp, info, gated):
         n += 3 if op[0] == "kadaneF" else 4
     n += 1  # stage 1
     if gated:
-        n += 3  # stage 2, boxcar, candidate read-back
+        n += 2  # stage 2, boxcar
     return n
 
 
@@ -287,7 +294,10 @@ def run_ours(args, wl):
     peak, peak_kind = measured_peaks()
     achieved = nb_total[top] / (cls_ms[top] / 1e3) / 1e9
     roof = {"bound": "hbm", "kernel": names[top], "achieved": achieved, "peak": peak,
-            "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+            "unit": "GB/s", "frac": achieved / peak,
+            "traffic": PROFILED_TRAFFIC.get((wl.name, args.precision, names[top])),
+            "traffic_source": ("profiles/traffic_nchan4096_n2M_rfi_dm3000.md (ncu, bytes per launch)"
+                               if (wl.name, args.precision, names[top]) in PROFILED_TRAFFIC else None),
             "peak_source": peak_kind,
             "class_ms": {names[c]: float(cls_ms[c]) for c in range(5)},
             "class_launches": {names[c]: int(cls_n[c]) for c in range(5)},

@@ -7,8 +7,8 @@
  *   history copy -> unpack+downsample -> equalize -> baseline -> zap -> rfilist ops ->
  *   stage 1 (ring) -> [gate, boxcar.cpp:161] stage 2 -> boxcar+threshold -> async D2H.
  * Candidate buffers rotate over NSLOT slots per (beam,row) so the device runs ahead of the
- * host; a slot is harvested before it is reused and at txg_sync.  A read-back kernel writes
- * each block's candidates into host-mapped pinned memory (two buffers per slot); sorting them
+ * host; a slot is harvested before it is reused and at txg_sync.  Each block's candidates
+ * are copied into pinned memory (two buffers per slot) on a copy stream; sorting them
  * into Cluster::run order (cluster.cpp:91-112) and clustering run on worker threads, so the
  * launching thread only waits for the device.  Raw blocks from host memory are copied on a
  * second stream, overlapping the previous block's kernels.
@@ -61,8 +61,9 @@ struct Result;
 struct Slot {
     txg_cand *dcand = nullptr;              /* device [cap] */
     int *dcount = nullptr;                  /* device [2]: count, error code */
-    txg_cand *hbuf[2] = {nullptr, nullptr}; /* pinned, host-mapped [hcap] */
-    txg_cand *hbuf_dev[2] = {nullptr, nullptr};
+    txg_cand *hbuf[2] = {nullptr, nullptr}; /* pinned [hcap] */
+    long nread = 0;                         /* candidates copied into hbuf[buf] */
+    cudaEvent_t boxed = nullptr;            /* the block's candidate list is complete */
     std::shared_ptr<Result> reader[2];      /* result whose sort may still read hbuf[i] */
     int buf = 0;                            /* buffer of the pending block */
     long uses = 0;
@@ -188,6 +189,7 @@ struct BeamRow {
     bool overflow = false;
     int dev_error = 0;
     std::deque<ResultP> fifo; /* harvested blocks not yet popped */
+    long guess = 4096;        /* candidates to read back with the next gated block */
 };
 
 static constexpr size_t FIFO_MAX = 256;
@@ -217,6 +219,7 @@ struct txg_handle {
     std::vector<BeamPrep> prep;           /* [beam] */
     cudaStream_t st = nullptr;
     cudaStream_t cst = nullptr; /* host-to-device copies of raw blocks */
+    cudaStream_t dst = nullptr; /* device-to-host copies of candidates */
     uint8_t *raw[2] = {nullptr, nullptr};
     uint8_t *stage[2] = {nullptr, nullptr}; /* pinned staging for pageable host input */
     cudaEvent_t raw_free[2] = {nullptr, nullptr};   /* kernels done with raw[i] */
@@ -275,6 +278,7 @@ void free_all(txg_handle *h)
 {
     if (h->st) cudaStreamSynchronize(h->st);
     if (h->cst) cudaStreamSynchronize(h->cst);
+    if (h->dst) cudaStreamSynchronize(h->dst);
     if (h->pool) h->pool->shutdown();
     for (auto &beam : h->br)
         for (auto &b : beam)
@@ -283,6 +287,7 @@ void free_all(txg_handle *h)
                     if (sl.hbuf[i]) cudaFreeHost(sl.hbuf[i]);
                 if (sl.hcount) cudaFreeHost(sl.hcount);
                 if (sl.done) cudaEventDestroy(sl.done);
+                if (sl.boxed) cudaEventDestroy(sl.boxed);
                 for (auto &e : sl.ev)
                     if (e) cudaEventDestroy(e);
             }
@@ -295,6 +300,8 @@ void free_all(txg_handle *h)
     }
     if (h->st) cudaStreamDestroy(h->st);
     if (h->cst) cudaStreamDestroy(h->cst);
+    if (h->dst) cudaStreamDestroy(h->dst);
+    h->dst = nullptr;
     h->st = nullptr;
     h->cst = nullptr;
 }
@@ -395,7 +402,9 @@ int harvest(txg_handle *h, BeamRow &b, Slot &sl, const RowPlan &P)
         r->count = cnt;
         b.last_count = cnt;
         const long keep = std::min(cnt, h->cap);
-        const long pre = std::min(keep, h->hcap);
+        const long pre = std::min(keep, sl.nread);
+        /* next read-back of this row: this count with a margin */
+        b.guess = std::min(h->hcap, std::max(4096L, cnt + cnt / 4 + 1024));
         r->src = sl.hbuf[sl.buf];
         r->nsrc = pre;
         sl.reader[sl.buf] = r;
@@ -506,20 +515,29 @@ int run_block(txg_handle *h, int beam, const uint8_t *raw)
             if (rc) return rc;
             TXG_CUDA_TRY(cudaGetLastError());
             if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[5], h->st));
-            /* the buffer's previous reader (two uses of this slot ago) must be done */
+            /* read-back on the copy stream, overlapping the next kernels: the row's expected
+             * count of candidates (the rest, if any, is fetched at harvest) and the count.
+             * The buffer's previous reader (two uses of this slot ago) must be done. */
             sl.buf = (int)(sl.uses++ & 1);
             if (sl.reader[sl.buf]) {
                 h->pool->wait(*sl.reader[sl.buf]);
                 sl.reader[sl.buf].reset();
             }
-            launch_copy_cands(sl.dcand, sl.dcount, h->hcap, sl.hbuf_dev[sl.buf], h->st);
-            TXG_CUDA_TRY(cudaGetLastError());
-        } else if (timing) {
-            TXG_CUDA_TRY(cudaEventRecord(sl.ev[4], h->st));
-            TXG_CUDA_TRY(cudaEventRecord(sl.ev[5], h->st));
+            sl.nread = std::min(b.guess, h->hcap);
+            TXG_CUDA_TRY(cudaEventRecord(sl.boxed, h->st));
+            TXG_CUDA_TRY(cudaStreamWaitEvent(h->dst, sl.boxed, 0));
+            TXG_CUDA_TRY(cudaMemcpyAsync(sl.hbuf[sl.buf], sl.dcand, sl.nread * sizeof(txg_cand),
+                                         cudaMemcpyDeviceToHost, h->dst));
+            TXG_CUDA_TRY(cudaMemcpyAsync(sl.hcount, sl.dcount, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->dst));
+            TXG_CUDA_TRY(cudaEventRecord(sl.done, h->dst));
+        } else {
+            if (timing) {
+                TXG_CUDA_TRY(cudaEventRecord(sl.ev[4], h->st));
+                TXG_CUDA_TRY(cudaEventRecord(sl.ev[5], h->st));
+            }
+            TXG_CUDA_TRY(cudaMemcpyAsync(sl.hcount, sl.dcount, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+            TXG_CUDA_TRY(cudaEventRecord(sl.done, h->st));
         }
-        TXG_CUDA_TRY(cudaMemcpyAsync(sl.hcount, sl.dcount, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
-        TXG_CUDA_TRY(cudaEventRecord(sl.done, h->st));
         sl.pending = true;
         sl.gated = gated;
         sl.counter = counter;
@@ -662,7 +680,9 @@ int txg_create(const txg_plan *plan, txg_handle **out)
         delete h;
         return fail(TXG_ERR_CUDA, "cudaStreamCreate failed");
     }
-    if (cudaStreamCreateWithFlags(&h->cst, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaStreamCreateWithFlags(&h->cst, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h->dst, cudaStreamNonBlocking) != cudaSuccess) {
+        if (h->cst) cudaStreamDestroy(h->cst);
         cudaStreamDestroy(h->st);
         delete h;
         return fail(TXG_ERR_CUDA, "cudaStreamCreate failed");
@@ -734,17 +754,15 @@ int txg_create(const txg_plan *plan, txg_handle **out)
             for (auto &sl : b.slot) {
                 if ((rc = dalloc(h, &sl.dcand, (size_t)h->cap)) || (rc = dalloc(h, &sl.dcount, (size_t)2)))
                     return bail(rc);
-                for (int i = 0; i < 2; i++) {
-                    if (cudaHostAlloc((void **)&sl.hbuf[i], sizeof(txg_cand) * h->hcap, cudaHostAllocMapped) !=
+                for (int i = 0; i < 2; i++)
+                    if (cudaHostAlloc((void **)&sl.hbuf[i], sizeof(txg_cand) * h->hcap, cudaHostAllocDefault) !=
                         cudaSuccess)
                         return bail(fail(TXG_ERR_NOMEM, "pinned candidate buffer allocation failed"));
-                    if (cudaHostGetDevicePointer((void **)&sl.hbuf_dev[i], sl.hbuf[i], 0) != cudaSuccess)
-                        return bail(fail(TXG_ERR_CUDA, "pinned candidate buffer is not device-mapped"));
-                }
                 if (cudaHostAlloc((void **)&sl.hcount, 2 * sizeof(int), cudaHostAllocDefault) != cudaSuccess)
                     return bail(fail(TXG_ERR_NOMEM, "pinned count allocation failed"));
                 sl.hcount[0] = sl.hcount[1] = 0;
-                if (cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) != cudaSuccess)
+                if (cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) != cudaSuccess ||
+                    cudaEventCreateWithFlags(&sl.boxed, cudaEventDisableTiming) != cudaSuccess)
                     return bail(fail(TXG_ERR_CUDA, "event creation failed"));
                 if (h->flags & TXG_FLAG_TIMING)
                     for (auto &e : sl.ev)

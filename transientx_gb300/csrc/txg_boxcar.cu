@@ -280,24 +280,7 @@ k_boxcar(const float *__restrict__ tim, long ldt, long n, const int32_t *__restr
     }
 }
 
-/* First min(*count, cap) candidates into a host-mapped buffer (16-byte records). */
-__global__ void __launch_bounds__(256) k_copy_cands(const int4 *__restrict__ src,
-                                                    const int *__restrict__ count, long cap, int4 *dst)
-{
-    const long n = min((long)*count, cap);
-    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-        dst[i] = src[i];
-}
-
 } // namespace
-
-void launch_copy_cands(const txg_cand *src, const int *count, long cap, txg_cand *dst, cudaStream_t st)
-{
-    static_assert(sizeof(txg_cand) == sizeof(int4), "candidate records are 16 bytes");
-    if (cap <= 0) return;
-    const long blocks = std::min<long>((cap + 255) / 256, 304);
-    k_copy_cands<<<(unsigned)blocks, 256, 0, st>>>((const int4 *)src, count, cap, (int4 *)dst);
-}
 
 size_t boxcar_max_samples() { return (BX_SMEM_MAX) / sizeof(float); }
 

@@ -767,8 +767,8 @@ static void stage1_chunked(const float *xh, long ldh, long col0, int C, long N, 
 /* Resident launch shapes (threads per set x samples per thread, thread sets x groups each):
  *   FP32 windows: 0 = 256x2 4x8 (default), 1 = 256x2 1x16, 2 = 512x1 1x16, 3 = 256x2 2x8,
  *                 4 = 256x2 2x16, 5 = 256x1 2x8, 6 = 256x2 4x4
- *   16-bit pairs: 0 = 256x1 4x8 (default), 1 = 256x1 1x16, 2 = 256x1 2x8, 3 = 256x1 2x16,
- *                 4 = 256x1 4x4, 5 = 128x1 4x8, 6 = 128x2 4x8
+ *   16-bit pairs: 0 = 128x2 4x8 (default), 1 = 256x1 1x16, 2 = 256x1 2x8, 3 = 256x1 2x16,
+ *                 4 = 256x1 4x4, 5 = 128x1 4x8, 6 = 256x1 4x8
  * (measured on the 4096-channel workload: more warps per SM over the same resident window
  * pay until the per-thread delay loads dominate).  A shape whose windows do not fit falls back
  * to 1x16, then to the chunked kernel. */
@@ -789,8 +789,8 @@ static void stage1_dispatch(const float *xh, const __half *x16, long ldh, long c
             case 3: done = stage1p_try<T, 256, 1, 2, 16>(TXG_PARGS); break;
             case 4: done = stage1p_try<T, 256, 1, 4, 4>(TXG_PARGS); break;
             case 5: done = stage1p_try<T, 128, 1, 4, 8>(TXG_PARGS); break;
-            case 6: done = stage1p_try<T, 128, 2, 4, 8>(TXG_PARGS); break;
-            default: done = stage1p_try<T, 256, 1, 4, 8>(TXG_PARGS); break;
+            case 6: done = stage1p_try<T, 256, 1, 4, 8>(TXG_PARGS); break;
+            default: done = stage1p_try<T, 128, 2, 4, 8>(TXG_PARGS); break;
             }
             if (!done) done = stage1p_try<T, 256, 1, 1, 16>(TXG_PARGS);
         }

@@ -96,8 +96,6 @@ int launch_boxcar(const float *tim, long ldt, long ndm, long n, const int32_t *v
                   int iqr, int avx2_tail, float thre, txg_cand *cand, int *ncand, long cap,
                   float *mxS, int32_t *mxwn, int *err, cudaStream_t st);
 size_t boxcar_max_samples();
-/* copy min(*count, cap) candidates to a host-mapped buffer (dst is its device address) */
-void launch_copy_cands(const txg_cand *src, const int *count, long cap, txg_cand *dst, cudaStream_t st);
 
 } // namespace txg
 
