@@ -32,7 +32,15 @@ typedef enum {
     TXG_ERR_UNSUPPORTED = -8   /* option not implemented for these sizes */
 } txg_status;
 
-typedef enum { TXG_RFI_KADANEF = 1, TXG_RFI_ZDOT = 2 } txg_rfi_kind;
+/* rfilist entries (singlepulse.cpp:298-325): kadaneF td fd, zdot, mask td fd, kadaneT td fd,
+ * zero */
+typedef enum {
+    TXG_RFI_KADANEF = 1,
+    TXG_RFI_ZDOT = 2,
+    TXG_RFI_MASK = 3,
+    TXG_RFI_KADANET = 4,
+    TXG_RFI_ZERO = 5
+} txg_rfi_kind;
 
 typedef enum {
     TXG_PREC_FP32 = 0,         /* subband series and prefix sums in FP32 (reference arithmetic) */
@@ -71,7 +79,10 @@ typedef struct {
     double radius_smearing;    /* Cluster::run arguments (singlepulse.cpp:332): radius in s */
     int32_t maxncand, minpts;
     int32_t drop;              /* remove_cand_with_maxwidth */
+    float threMask;            /* mask outlier threshold in IQR units (singlepulse.cpp:302) */
+    float threKadaneT;         /* S/N threshold of kadaneT (squared before use, :312) */
     int32_t pad;
+    double bandlimitKT;        /* kadaneT minimum band in MHz (:312) */
 } txg_row;
 
 typedef struct {
@@ -159,8 +170,10 @@ int txg_get_timdata(txg_handle *h, int32_t beam, int32_t row, int64_t idm0, int6
                     float *out);
 
 /* The row's preprocessed block after the rfilist ([nchans][ndump], TXG_FLAG_KEEP_SERIES),
- * and the kadaneF windows of rfilist entry irfi ([nchans/fd][4]: start,end of the positive
- * and negative window in block samples, -1 if not zapped). */
+ * and the zapped windows of rfilist entry irfi: kadaneF [nchans/fd][4] (start,end of the
+ * positive and negative window in block samples, -1 if not zapped); kadaneT [ndump/td][4]
+ * (start,end of the positive and negative band in channels per downsampled sample); mask
+ * [1][4] (number of zapped pixels, 0, 0, 0). */
 int txg_get_block(txg_handle *h, int32_t beam, int32_t row, float *out);
 int txg_get_zap_ranges(txg_handle *h, int32_t beam, int32_t row, int32_t irfi, int32_t *out,
                        int64_t cap);

@@ -43,6 +43,8 @@ struct SinglePulse {
     std::vector<std::vector<std::string>> rfilist;
     double widthlimit = 50e-3;
     float threKadaneF = 7.f;
+    float threMask = 10.f, threKadaneT = 7.f; /* CLI defaults, dedisperse_fil.cpp:79-83 */
+    double bandlimitKT = 10.;
     double dms = 0., ddm = 1.;
     long ndm = 200;
     double overlap = 0.;
@@ -72,6 +74,13 @@ struct SinglePulse {
             } else if (op[0] == "zdot") {
                 r.rfi_kind[i] = TXG_RFI_ZDOT;
                 r.rfi_td[i] = r.rfi_fd[i] = 1;
+            } else if ((op[0] == "mask" || op[0] == "kadaneT") && op.size() >= 3) {
+                r.rfi_kind[i] = op[0] == "mask" ? TXG_RFI_MASK : TXG_RFI_KADANET;
+                r.rfi_td[i] = std::stoi(op[1]);
+                r.rfi_fd[i] = std::stoi(op[2]);
+            } else if (op[0] == "zero") {
+                r.rfi_kind[i] = TXG_RFI_ZERO;
+                r.rfi_td[i] = r.rfi_fd[i] = 1;
             } else {
                 throw Error(TXG_ERR_UNSUPPORTED, "rfilist entry " + op[0] + " is not implemented");
             }
@@ -83,6 +92,9 @@ struct SinglePulse {
         }
         r.threKadaneF = threKadaneF;
         r.widthlimit = widthlimit;
+        r.threMask = threMask;
+        r.threKadaneT = threKadaneT;
+        r.bandlimitKT = bandlimitKT;
         r.dms = dms;
         r.ddm = ddm;
         r.ndm = ndm;

@@ -23,6 +23,9 @@ u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
 
 RFI_KADANEF = 1
 RFI_ZDOT = 2
+RFI_MASK = 3
+RFI_KADANET = 4
+RFI_ZERO = 5
 
 
 def build(ref: bool = True) -> None:
@@ -59,6 +62,7 @@ class Row(C.Structure):
         ("ndm", C.c_long), ("overlap", C.c_double), ("nsub", C.c_int), ("group", C.c_int),
         ("minw", C.c_float), ("maxw", C.c_float), ("snrloss", C.c_float), ("iqr", C.c_int),
         ("avx2_tail", C.c_int), ("thre", C.c_float), ("zapthre", C.c_float), ("fp64", C.c_int),
+        ("threMask", C.c_float), ("threKadaneT", C.c_float), ("bandlimitKT", C.c_double),
     ]
 
 
@@ -73,6 +77,12 @@ def make_row(**kw) -> Row:
             r.rfi_kind[i], r.rfi_td[i], r.rfi_fd[i] = RFI_KADANEF, int(op[1]), int(op[2])
         elif op[0] == "zdot":
             r.rfi_kind[i], r.rfi_td[i], r.rfi_fd[i] = RFI_ZDOT, 1, 1
+        elif op[0] == "mask":
+            r.rfi_kind[i], r.rfi_td[i], r.rfi_fd[i] = RFI_MASK, int(op[1]), int(op[2])
+        elif op[0] == "kadaneT":
+            r.rfi_kind[i], r.rfi_td[i], r.rfi_fd[i] = RFI_KADANET, int(op[1]), int(op[2])
+        elif op[0] == "zero":
+            r.rfi_kind[i], r.rfi_td[i], r.rfi_fd[i] = RFI_ZERO, 1, 1
         else:
             raise ValueError(f"unsupported rfi op {op}")
     zap = kw.get("zap", [])
@@ -89,6 +99,9 @@ def make_row(**kw) -> Row:
     r.avx2_tail = int(kw.get("avx2_tail", False))
     r.thre = kw.get("thre", 7.0)
     r.zapthre = kw.get("zapthre", -1.0)
+    r.threMask = kw.get("threMask", 10.0)
+    r.threKadaneT = kw.get("threKadaneT", 7.0)
+    r.bandlimitKT = kw.get("bandlimitKT", 10.0)
     r.fp64 = int(kw.get("fp64", False))
     return r
 
@@ -127,6 +140,12 @@ def lib() -> C.CDLL:
     L.txo_kadaneF.argtypes = [f32p, C.c_int, C.c_long, C.c_long, C.c_int, C.c_int, C.c_float,
                               C.c_long, i32p]
     L.txo_zdot.argtypes = [f32p, C.c_int, C.c_long, C.c_long]
+    L.txo_kadaneT.restype = C.c_int
+    L.txo_kadaneT.argtypes = [f32p, C.c_int, C.c_long, C.c_long, C.c_int, C.c_int, C.c_float,
+                              C.c_long, i32p]
+    L.txo_mask.restype = C.c_int
+    L.txo_mask.argtypes = [f32p, C.c_int, C.c_long, C.c_long, C.c_int, C.c_int, C.c_float, f32p]
+    L.txo_zero.argtypes = [f32p, C.c_int, C.c_long, C.c_long, C.c_void_p]
     L.txo_boxcar_match.argtypes = [f32p, C.c_long, i32p, C.c_int, C.c_int, C.c_int, f32p, i32p]
     L.txo_boxcar_run.argtypes = [f32p, C.c_long, C.c_long, i32p, C.c_int, C.c_int, C.c_int,
                                  f32p, i32p]
@@ -251,6 +270,28 @@ def kadaneF(x, tdk, fdk, thr, wnlimit):
     ranges = np.zeros((x.shape[0] // fdk, 4), np.int32)
     lib().txo_kadaneF(x, x.shape[0], x.shape[1], x.shape[1], tdk, fdk, thr, wnlimit, ranges)
     return x, ranges
+
+
+def kadaneT(x, tdk, fdk, thr, bwlimit):
+    x = np.array(x, np.float32, order="C", copy=True)
+    ranges = np.zeros((x.shape[1] // tdk, 4), np.int32)
+    n = lib().txo_kadaneT(x, x.shape[0], x.shape[1], x.shape[1], tdk, fdk, thr, bwlimit, ranges)
+    return x, ranges, n
+
+
+def mask(x, tdk, fdk, thr):
+    """Returns (x, number of zapped pixels, [Q1, Q3, lo, hi])."""
+    x = np.array(x, np.float32, order="C", copy=True)
+    q = np.zeros(4, np.float32)
+    n = lib().txo_mask(x, x.shape[0], x.shape[1], x.shape[1], tdk, fdk, thr, q)
+    return x, n, q
+
+
+def zero(x, live=None):
+    x = np.array(x, np.float32, order="C", copy=True)
+    live = np.ones(x.shape[0], np.uint8) if live is None else np.ascontiguousarray(live, np.uint8)
+    lib().txo_zero(x, x.shape[0], x.shape[1], x.shape[1], live.ctypes.data)
+    return x
 
 
 def zdot(x):

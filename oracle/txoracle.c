@@ -362,6 +362,128 @@ int txo_kadaneF(float *x, int nchan, long n, long ldx, int tdk, int fdk, float t
     return nzapped;
 }
 
+static int cmp_float(const void *a, const void *b);
+
+/* Sum-downsample of kadaneF (candidate.cpp:727-739): d[j*nds + i] = sum over k < fdk (outer)
+ * and t < tdk (inner) of x[j*fdk + k][i*tdk + t], from 0.0f. */
+static void ds_sum(const float *x, long ldx, int cds, long nds, int tdk, int fdk, float *d)
+{
+#pragma omp parallel for num_threads(nthr())
+    for (int j = 0; j < cds; j++)
+        for (long i = 0; i < nds; i++) {
+            float acc = 0.f;
+            for (int k = 0; k < fdk; k++)
+                for (int t = 0; t < tdk; t++) acc = acc + x[((long)j * fdk + k) * ldx + i * tdk + t];
+            d[(long)j * nds + i] = acc;
+        }
+}
+
+/* kadaneT, the rfilist entry `kadaneT td fd` (singlepulse.cpp:310-313; the XLibs source is
+ * not in the reference tree, the CLI describes a band limit in MHz and an S/N threshold,
+ * dedisperse_fil.cpp:79,83).  Defined here as kadaneF with time and frequency exchanged:
+ * on the td x fd sum-downsampled block, each downsampled sample i scans its channels in
+ * ascending order for the maximum-sum band (txo_kadane), positive and negated; the band is
+ * zapped (set to the mean, 0) when it spans more than bwlimit downsampled channels and
+ * boxsum^2/(wn*td*fd) > thr (the squared threshold).  ranges[4*i + 0..3] receives the
+ * [start, end) channels of the positive and negative band, or -1,-1.  Returns the number of
+ * zapped bands. */
+int txo_kadaneT(float *x, int nchan, long n, long ldx, int tdk, int fdk, float thr, long bwlimit,
+                int32_t *ranges)
+{
+    const long nds = n / tdk;
+    const int cds = nchan / fdk;
+    if (nds <= 0 || cds <= 0) return 0;
+    float *d = (float *)malloc(sizeof(float) * (size_t)cds * nds);
+    ds_sum(x, ldx, cds, nds, tdk, fdk, d);
+    const float var = (float)(tdk * fdk);
+    int nzapped = 0;
+#pragma omp parallel num_threads(nthr()) reduction(+ : nzapped)
+    {
+        float *y = (float *)malloc(sizeof(float) * cds);
+#pragma omp for
+        for (long i = 0; i < nds; i++)
+            for (int p = 0; p < 2; p++) {
+                for (int j = 0; j < cds; j++) y[j] = p == 0 ? d[(long)j * nds + i] : -d[(long)j * nds + i];
+                long start, end;
+                float boxsum = txo_kadane(y, cds, &start, &end);
+                long wn = end - start + 1;
+                float snr2 = 0.f;
+                if (wn > bwlimit) snr2 = boxsum * boxsum / ((float)wn * var);
+                if (snr2 > thr) {
+                    ranges[4 * i + 2 * p] = (int32_t)(start * fdk);
+                    ranges[4 * i + 2 * p + 1] = (int32_t)((end + 1) * fdk);
+                    nzapped++;
+                } else {
+                    ranges[4 * i + 2 * p] = -1;
+                    ranges[4 * i + 2 * p + 1] = -1;
+                }
+            }
+        free(y);
+    }
+#pragma omp parallel for num_threads(nthr())
+    for (long i = 0; i < nds; i++)
+        for (int p = 0; p < 2; p++) {
+            int32_t a = ranges[4 * i + 2 * p], b = ranges[4 * i + 2 * p + 1];
+            if (a < 0) continue;
+            for (int c = a; c < b; c++)
+                for (int t = 0; t < tdk; t++) x[(long)c * ldx + i * tdk + t] = 0.f;
+        }
+    free(d);
+    return nzapped;
+}
+
+/* Mask filter, the rfilist entry `mask td fd` (singlepulse.cpp:300-303; docs
+ * pipeline/rfi_mitigation.rst "Mask filter" and its diagram: downsample by td x fd, remove
+ * pixel outliers by IQR; the XLibs source is not in the reference tree).  Defined here with
+ * the quartile rule of the channel zap (candidate.cpp:622-652): over all pixels d of the
+ * sum-downsampled block, Q1 = sorted[n/4], Q3 = sorted[n-1-n/4], R = Q3 - Q1; pixels below
+ * Q1 - thr*R or above Q3 + thr*R are zapped (their td x fd cells set to the mean, 0).
+ * quart (4 floats, may be NULL) receives Q1, Q3 and the two limits.  Returns the number of
+ * zapped pixels. */
+int txo_mask(float *x, int nchan, long n, long ldx, int tdk, int fdk, float thr, float *quart)
+{
+    const long nds = n / tdk;
+    const int cds = nchan / fdk;
+    if (nds <= 0 || cds <= 0) return 0;
+    const long np = (long)cds * nds;
+    float *d = (float *)malloc(sizeof(float) * np);
+    float *srt = (float *)malloc(sizeof(float) * np);
+    ds_sum(x, ldx, cds, nds, tdk, fdk, d);
+    memcpy(srt, d, sizeof(float) * np);
+    qsort(srt, np, sizeof(float), cmp_float);
+    const float q1 = srt[np / 4], q3 = srt[np - 1 - np / 4];
+    const float r = q3 - q1;
+    const float lo = q1 - thr * r, hi = q3 + thr * r;
+    if (quart) {
+        quart[0] = q1;
+        quart[1] = q3;
+        quart[2] = lo;
+        quart[3] = hi;
+    }
+    int nz = 0;
+#pragma omp parallel for num_threads(nthr()) reduction(+ : nz)
+    for (int j = 0; j < cds; j++)
+        for (long i = 0; i < nds; i++) {
+            const float v = d[(long)j * nds + i];
+            if (v < lo || v > hi) {
+                nz++;
+                for (int k = 0; k < fdk; k++)
+                    for (int t = 0; t < tdk; t++) x[((long)j * fdk + k) * ldx + i * tdk + t] = 0.f;
+            }
+        }
+    free(d);
+    free(srt);
+    return nz;
+}
+
+/* Zero-DM filter, the rfilist entry `zero` (singlepulse.cpp:320-323; docs usage: "zero
+ * (zero-DM filter)"): the live-channel mean series is subtracted from every live channel,
+ * i.e. BaseLine with a one-sample window. */
+void txo_zero(float *x, int nchan, long n, long ldx, const uint8_t *live)
+{
+    txo_baseline(x, nchan, n, ldx, 1, live);
+}
+
 /* Zero-DM matched filter (src/singlepulse/candidate.cpp:831-897): normalise every channel,
  * form the channel-mean series s, remove each channel's least-squares fit alpha*s+beta. */
 void txo_zdot(float *x, int nchan, long n, long ldx)
@@ -951,9 +1073,14 @@ txo_sp *txo_sp_create(const txo_row *row, int nchan, const double *freqs, double
     sp->x = (float *)calloc((size_t)sp->nchan * sp->ldx, sizeof(float));
     sp->mask = (uint8_t *)calloc(nchan, 1);
     sp->live = (uint8_t *)calloc(sp->nchan, 1);
-    for (int r = 0; r < row->nrfi && r < 8; r++)
+    for (int r = 0; r < row->nrfi && r < 8; r++) {
         if (row->rfi_kind[r] == TXO_RFI_KADANEF)
             sp->ranges[r] = (int32_t *)calloc((size_t)4 * (sp->nchan / row->rfi_fd[r] + 1), 4);
+        else if (row->rfi_kind[r] == TXO_RFI_KADANET)
+            sp->ranges[r] = (int32_t *)calloc((size_t)4 * (sp->n / row->rfi_td[r] + 1), 4);
+        else if (row->rfi_kind[r] == TXO_RFI_MASK)
+            sp->ranges[r] = (int32_t *)calloc(4, 4);
+    }
     sp->dd = txo_dedisp_create(sp->nchan, sp->freqs, sp->tsamp, sp->n, row->dms, row->ddm,
                                row->ndm, row->overlap, row->nsub, row->group);
     if (!sp->dd) {
@@ -1001,6 +1128,16 @@ int txo_sp_run(txo_sp *sp, const uint8_t *raw)
                         wnlimit, sp->ranges[r]);
         } else if (row->rfi_kind[r] == TXO_RFI_ZDOT) {
             txo_zdot(sp->x, sp->nchan, sp->n, sp->ldx);
+        } else if (row->rfi_kind[r] == TXO_RFI_KADANET) {
+            const double chbw = sp->nchan > 1 ? fabs(sp->freqs[1] - sp->freqs[0]) : 0.;
+            const long bwlimit = chbw > 0. ? (long)(row->bandlimitKT / (chbw * row->rfi_fd[r])) : 0;
+            txo_kadaneT(sp->x, sp->nchan, sp->n, sp->ldx, row->rfi_td[r], row->rfi_fd[r],
+                        row->threKadaneT * row->threKadaneT, bwlimit, sp->ranges[r]);
+        } else if (row->rfi_kind[r] == TXO_RFI_MASK) {
+            sp->ranges[r][0] = txo_mask(sp->x, sp->nchan, sp->n, sp->ldx, row->rfi_td[r],
+                                        row->rfi_fd[r], row->threMask, NULL);
+        } else if (row->rfi_kind[r] == TXO_RFI_ZERO) {
+            txo_zero(sp->x, sp->nchan, sp->n, sp->ldx, sp->live);
         }
     }
     int gated = txo_dedisp_run(sp->dd, sp->x, sp->ldx);
@@ -1036,7 +1173,9 @@ const float *txo_sp_block(const txo_sp *sp, long *ldx, int *nchan, long *n)
 const int32_t *txo_sp_zap_ranges(const txo_sp *sp, int irfi, int *nrows)
 {
     if (irfi < 0 || irfi >= 8 || !sp->ranges[irfi]) return NULL;
-    *nrows = sp->nchan / sp->row.rfi_fd[irfi];
+    const int kind = sp->row.rfi_kind[irfi];
+    *nrows = kind == TXO_RFI_KADANEF ? sp->nchan / sp->row.rfi_fd[irfi]
+             : kind == TXO_RFI_KADANET ? (int)(sp->n / sp->row.rfi_td[irfi]) : 1;
     return sp->ranges[irfi];
 }
 

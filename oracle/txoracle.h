@@ -52,6 +52,10 @@ void txo_zap_channels(float *x, int nchan, long n, long ldx, const double *freqs
 int txo_kadaneF(float *x, int nchan, long n, long ldx, int tdk, int fdk, float thr,
                 long wnlimit, int32_t *ranges);
 void txo_zdot(float *x, int nchan, long n, long ldx);
+int txo_kadaneT(float *x, int nchan, long n, long ldx, int tdk, int fdk, float thr, long bwlimit,
+                int32_t *ranges);
+int txo_mask(float *x, int nchan, long n, long ldx, int tdk, int fdk, float thr, float *quart);
+void txo_zero(float *x, int nchan, long n, long ldx, const uint8_t *live);
 
 /* ---- boxcar over dedispersed series (boxcar.cpp:180-296) ------------------------------ */
 void txo_boxcar_match(const float *tim, long n, const int *vwn, int nw, int iqr,
@@ -96,7 +100,7 @@ void txo_dedisp_set_fp64(txo_dedisp *dd);
 const double *txo_dedisp_timdata64(const txo_dedisp *dd);
 
 /* ---- one ddplan row, the SinglePulse::run chain --------------------------------------- */
-enum { TXO_RFI_KADANEF = 1, TXO_RFI_ZDOT = 2 };
+enum { TXO_RFI_KADANEF = 1, TXO_RFI_ZDOT = 2, TXO_RFI_MASK = 3, TXO_RFI_KADANET = 4, TXO_RFI_ZERO = 5 };
 
 typedef struct {
     int td, fd;
@@ -116,6 +120,8 @@ typedef struct {
     float thre;
     float zapthre;
     int fp64; /* dedispersion sums and boxcar in double: the FP64 reference */
+    float threMask, threKadaneT;
+    double bandlimitKT;
 } txo_row;
 
 typedef struct txo_sp txo_sp;

@@ -38,7 +38,8 @@ def oracle_rows(oracle, rows, fil, ndump, tx, avx2=False, zapthre=4.0):
                               ddm=sp.ddm, ndm=sp.ndm, overlap=sp.overlap, nsub=info.nsub,
                               group=info.dm_group, minw=sp.minw, maxw=sp.maxw,
                               snrloss=sp.snrloss, iqr=sp.iqr, thre=sp.thre, avx2_tail=avx2,
-                              zapthre=zapthre)
+                              zapthre=zapthre, threMask=sp.threMask,
+                              threKadaneT=sp.threKadaneT, bandlimitKT=sp.bandlimitKT)
         out.append(oracle.SinglePulseRow(row, fil.freqs, fil.tsamp, ndump))
     return out
 
@@ -76,6 +77,46 @@ def test_pipeline_fp32_matches_oracle(tx, oracle, avx2, zapthre):
                 ref = oracle.threshold_scan(o.mxS(), o.mxwn(), rows[r].thre)
                 assert_cands_close(s.candidates(r), ref, rows[r].thre)
     assert ngated >= 4
+
+
+RFI_LISTS = {
+    "mask": [["mask", "4", "2"]],
+    "mask11": [["mask", "1", "1"]],
+    "kadaneT": [["kadaneT", "2", "2"]],
+    "zero": [["zero"]],
+    "all": [["kadaneF", "8", "4"], ["mask", "2", "4"], ["kadaneT", "4", "4"], ["zero"], ["zdot"]],
+}
+
+
+@pytest.mark.parametrize("name", list(RFI_LISTS))
+def test_rfi_options_match_oracle(tx, oracle, name):
+    """mask / kadaneT / zero rfilist entries: preprocessed block, zapped windows and the
+    dedispersed series bit-exact against the oracle, every block; each entry must fire."""
+    fil, rows, ndump = small_workload()
+    for sp in rows:
+        sp.rfilist = [list(op) for op in RFI_LISTS[name]]
+    flags = tx.FLAG_KEEP_SERIES
+    orows = oracle_rows(oracle, rows, fil, ndump, tx)
+    fired = {}
+    with tx.Search(rows, fil.nchans, fil.tsamp, fil.freqs, ndump, flags=flags, zapthre=4.0) as s:
+        for b in range(fil.nsamples // ndump):
+            raw = fil.generate(b * ndump, ndump)
+            s.push_block(raw)
+            s.sync()
+            for r, o in enumerate(orows):
+                gated = o.run(raw)
+                np.testing.assert_array_equal(s.block(r), o.block(), err_msg=f"{name} block {b} row {r}")
+                for q, op in enumerate(rows[r].rfilist):
+                    if op[0] in ("mask", "kadaneT", "kadaneF"):
+                        zr = s.zap_ranges(q, r)
+                        np.testing.assert_array_equal(zr, o.zap_ranges(q), err_msg=f"{name} {op}")
+                        hit = zr[0, 0] if op[0] == "mask" else int((zr[:, 0] >= 0).sum() + (zr[:, 2] >= 0).sum())
+                        fired[op[0]] = fired.get(op[0], 0) + int(hit)
+                if gated:
+                    np.testing.assert_array_equal(s.timdata(r), o.timdata(), err_msg=f"{name} tim {b} {r}")
+    for op in RFI_LISTS[name]:
+        if op[0] in ("mask", "kadaneT"):
+            assert fired.get(op[0], 0) > 0, (name, op, fired)
 
 
 def test_skzap_catches_sinusoids(tx, oracle):

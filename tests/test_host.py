@@ -73,7 +73,11 @@ def test_plan_rejects_bad_rows(tx):
     with pytest.raises(TxgError):
         tx.describe_row([SinglePulse(dms=-1.0, ndm=10)], 0, 64, 1e-4, f, 1000)
     with pytest.raises(TxgError):
-        tx.describe_row([SinglePulse(ndm=10, rfilist=[["mask", "2", "2"]])], 0, 64, 1e-4, f, 1000)
+        tx.describe_row([SinglePulse(ndm=10, rfilist=[["mask", "0", "2"]])], 0, 64, 1e-4, f, 1000)
+    with pytest.raises(TxgError):
+        tx.describe_row([SinglePulse(ndm=10, rfilist=[["clip", "2", "2"]])], 0, 64, 1e-4, f, 1000)
+    for op in (["mask", "2", "2"], ["kadaneT", "4", "2"], ["zero"]):
+        tx.describe_row([SinglePulse(ndm=10, rfilist=[op])], 0, 64, 1e-4, f, 1000)
 
 
 def test_product_cluster_matches_reference_golden(tx, golden):

@@ -26,7 +26,7 @@ LIB_PATH = os.path.join(PKG, "libtxgpu.so")
 OK = 0
 ERR_ARG, ERR_NOMEM, ERR_CUDA, ERR_OVERFLOW = -1, -2, -3, -4
 ERR_TIMEOUT, ERR_STATE, ERR_NODEVICE, ERR_UNSUPPORTED = -5, -6, -7, -8
-RFI_KADANEF, RFI_ZDOT = 1, 2
+RFI_KADANEF, RFI_ZDOT, RFI_MASK, RFI_KADANET, RFI_ZERO = 1, 2, 3, 4, 5
 PREC_FP32, PREC_BF16, PREC_FP16 = 0, 1, 2
 FLAG_AVX2_TAIL, FLAG_DENSE, FLAG_KEEP_SERIES, FLAG_TIMING, FLAG_CLUSTER = 1, 2, 4, 8, 16
 PRECISIONS = {"fp32": PREC_FP32, "bf16": PREC_BF16, "fp16": PREC_FP16}
@@ -47,7 +47,8 @@ class txg_row(C.Structure):
         ("ndm", C.c_int64), ("overlap", C.c_double), ("minw", C.c_float), ("maxw", C.c_float),
         ("snrloss", C.c_float), ("iqr", C.c_int32), ("thre", C.c_float), ("nsub", C.c_int32),
         ("dm_group", C.c_int32), ("radius_smearing", C.c_double), ("maxncand", C.c_int32),
-        ("minpts", C.c_int32), ("drop", C.c_int32), ("pad", C.c_int32),
+        ("minpts", C.c_int32), ("drop", C.c_int32), ("threMask", C.c_float),
+        ("threKadaneT", C.c_float), ("pad", C.c_int32), ("bandlimitKT", C.c_double),
     ]
 
 
@@ -160,6 +161,9 @@ class SinglePulse:
     rfilist: List[List[str]] = field(default_factory=list)
     widthlimit: float = 50e-3
     threKadaneF: float = 7.0
+    threMask: float = 10.0
+    threKadaneT: float = 7.0
+    bandlimitKT: float = 10.0
     dms: float = 0.0
     ddm: float = 1.0
     ndm: int = 200
@@ -189,12 +193,19 @@ class SinglePulse:
                 r.rfi_kind[i], r.rfi_td[i], r.rfi_fd[i] = RFI_KADANEF, int(op[1]), int(op[2])
             elif op[0] == "zdot":
                 r.rfi_kind[i], r.rfi_td[i], r.rfi_fd[i] = RFI_ZDOT, 1, 1
+            elif op[0] == "mask":
+                r.rfi_kind[i], r.rfi_td[i], r.rfi_fd[i] = RFI_MASK, int(op[1]), int(op[2])
+            elif op[0] == "kadaneT":
+                r.rfi_kind[i], r.rfi_td[i], r.rfi_fd[i] = RFI_KADANET, int(op[1]), int(op[2])
+            elif op[0] == "zero":
+                r.rfi_kind[i], r.rfi_td[i], r.rfi_fd[i] = RFI_ZERO, 1, 1
             else:
                 raise TxgError(ERR_UNSUPPORTED, f"rfilist entry {op[0]!r} is not implemented")
         r.nzap = len(self.zaplist)
         for i, (a, b) in enumerate(self.zaplist):
             r.zap[i][0], r.zap[i][1] = a, b
         r.threKadaneF, r.widthlimit = self.threKadaneF, self.widthlimit
+        r.threMask, r.threKadaneT, r.bandlimitKT = self.threMask, self.threKadaneT, self.bandlimitKT
         r.dms, r.ddm, r.ndm, r.overlap = self.dms, self.ddm, self.ndm, self.overlap
         r.minw, r.maxw, r.snrloss = self.minw, self.maxw, self.snrloss
         r.iqr, r.thre = int(self.iqr), self.thre
@@ -402,9 +413,17 @@ class Search:
         return out
 
     def zap_ranges(self, irfi: int, row: int = 0, beam: int = 0) -> np.ndarray:
+        """kadaneF: [nchans/fd][4] sample windows; kadaneT: [ndump/td][4] channel bands;
+        mask: [1][4] with the number of zapped pixels first."""
         i = self.row_info(row, beam)
-        fd = int(self.rows[row].rfilist[irfi][2])
-        out = np.zeros((i.nchans // fd, 4), np.int32)
+        op = self.rows[row].rfilist[irfi]
+        if op[0] == "mask":
+            n = 1
+        elif op[0] == "kadaneT":
+            n = i.ndump // int(op[1])
+        else:
+            n = i.nchans // int(op[2])
+        out = np.zeros((n, 4), np.int32)
         _check(load_library().txg_get_zap_ranges(self.h, beam, row, irfi, _ptr(out), out.size),
                "zap_ranges")
         return out

@@ -171,6 +171,7 @@ struct BeamRow {
     int cur = 0;
     float *ds = nullptr;
     int32_t *ranges[8] = {nullptr};
+    uint32_t *sel = nullptr; /* mask: quartile selection state */
     float *z = nullptr, *b = nullptr, *s = nullptr;
     double *sst = nullptr;
     uint8_t *live = nullptr;
@@ -487,6 +488,17 @@ int run_block(txg_handle *h, int beam, const uint8_t *raw)
                               P.kad_wnlimit[q], b.ds, b.ranges[q], h->st);
             else if (P.cfg.rfi_kind[q] == TXG_RFI_ZDOT)
                 launch_zdot(x, P.ldh, P.C, P.N, b.s, b.sst, h->st);
+            else if (P.cfg.rfi_kind[q] == TXG_RFI_KADANET)
+                launch_kadaneT(x, P.ldh, P.C, P.N, P.cfg.rfi_td[q], P.cfg.rfi_fd[q], P.kadT_thr,
+                               P.kad_wnlimit[q], b.ds, b.ranges[q], h->st);
+            else if (P.cfg.rfi_kind[q] == TXG_RFI_MASK)
+                launch_mask(x, P.ldh, P.C, P.N, P.cfg.rfi_td[q], P.cfg.rfi_fd[q], P.mask_thr, b.ds,
+                            b.sel, b.ranges[q], h->st);
+            else if (P.cfg.rfi_kind[q] == TXG_RFI_ZERO) {
+                /* zero-DM filter: the live-channel mean series off every live channel */
+                launch_colmean(x, P.ldh, P.C, P.N, b.live, b.z, h->st);
+                launch_sub_series(x, P.ldh, P.C, P.N, b.z, b.live, h->st);
+            }
         }
         /* 16-bit precisions: stage 1 reads an FP16 copy (history columns included) */
         if (b.x16) launch_to_half(xcur, P.ldh, P.C, P.H + P.N, b.x16, h->st);
@@ -731,12 +743,18 @@ int txg_create(const txg_plan *plan, txg_handle **out)
                 if ((rc = dalloc(h, &b.xh[i], (size_t)P.C * P.ldh))) return bail(rc);
             if (h->prec != TXG_PREC_FP32 && (rc = dalloc(h, &b.x16, (size_t)P.C * P.ldh))) return bail(rc);
             long kmax = 1;
-            for (int q = 0; q < P.cfg.nrfi; q++)
-                if (P.cfg.rfi_kind[q] == TXG_RFI_KADANEF) {
-                    long nds = P.N / P.cfg.rfi_td[q], cds = P.C / P.cfg.rfi_fd[q];
-                    kmax = std::max(kmax, nds * cds);
-                    if ((rc = dalloc(h, &b.ranges[q], (size_t)4 * (cds + 1)))) return bail(rc);
-                }
+            for (int q = 0; q < P.cfg.nrfi; q++) {
+                const int kind = P.cfg.rfi_kind[q];
+                if (kind != TXG_RFI_KADANEF && kind != TXG_RFI_KADANET && kind != TXG_RFI_MASK) continue;
+                long nds = P.N / P.cfg.rfi_td[q], cds = P.C / P.cfg.rfi_fd[q];
+                kmax = std::max(kmax, nds * cds);
+                /* kadaneF: 4 per downsampled channel; kadaneT: 4 per downsampled sample;
+                 * mask: the zapped-pixel count */
+                const long nr = kind == TXG_RFI_KADANEF ? cds + 1 : kind == TXG_RFI_KADANET ? nds + 1 : 1;
+                if ((rc = dalloc(h, &b.ranges[q], (size_t)4 * nr))) return bail(rc);
+                if (kind == TXG_RFI_MASK && !b.sel && (rc = dalloc(h, &b.sel, (size_t)MASK_SEL_WORDS)))
+                    return bail(rc);
+            }
             if ((rc = dalloc(h, &b.ds, (size_t)kmax)) || (rc = dalloc(h, &b.z, (size_t)P.N)) ||
                 (rc = dalloc(h, &b.live, (size_t)P.C)) ||
                 (rc = dalloc(h, &b.b, (size_t)P.N)) || (rc = dalloc(h, &b.s, (size_t)P.N)) ||
@@ -942,9 +960,19 @@ int txg_get_zap_ranges(txg_handle *h, int32_t beam, int32_t row, int32_t irfi, i
     int rc = check_beam_row(h, beam, row);
     if (rc) return rc;
     const RowPlan &P = h->rp[row];
-    if (irfi < 0 || irfi >= P.cfg.nrfi || P.cfg.rfi_kind[irfi] != TXG_RFI_KADANEF)
-        return fail(TXG_ERR_ARG, "rfilist entry is not a kadaneF");
-    const long rows = P.C / P.cfg.rfi_fd[irfi];
+    if (irfi < 0 || irfi >= P.cfg.nrfi)
+        return fail(TXG_ERR_ARG, "rfilist entry out of range");
+    const int kind = P.cfg.rfi_kind[irfi];
+    if (kind != TXG_RFI_KADANEF && kind != TXG_RFI_KADANET && kind != TXG_RFI_MASK)
+        return fail(TXG_ERR_ARG, "rfilist entry is not a kadaneF, kadaneT or mask");
+    if (kind == TXG_RFI_MASK) {
+        if (!out || cap < 4) return fail(TXG_ERR_ARG, "output too small");
+        TXG_CUDA_TRY(cudaStreamSynchronize(h->st));
+        TXG_CUDA_TRY(cudaMemcpy(out, h->br[beam][row].ranges[irfi], sizeof(int32_t), cudaMemcpyDeviceToHost));
+        out[1] = out[2] = out[3] = 0;
+        return TXG_OK;
+    }
+    const long rows = kind == TXG_RFI_KADANEF ? P.C / P.cfg.rfi_fd[irfi] : P.N / P.cfg.rfi_td[irfi];
     if (!out || cap < 4 * rows) return fail(TXG_ERR_ARG, "output too small");
     TXG_CUDA_TRY(cudaStreamSynchronize(h->st));
     TXG_CUDA_TRY(cudaMemcpy(out, h->br[beam][row].ranges[irfi], 4 * rows * sizeof(int32_t),

@@ -40,8 +40,11 @@ struct RowPlan {
     int maxwn = 0;
     long bl_nw = 0;       /* baseline window in samples, 0 = off */
     std::vector<int32_t> zap_chan;
-    long kad_wnlimit[8] = {0};
-    float kad_thr = 0.f;
+    long kad_wnlimit[8] = {0}; /* kadaneF: minimum window (samples); kadaneT: minimum band
+                                * (channels), both downsampled */
+    float kad_thr = 0.f;       /* threKadaneF^2 */
+    float kadT_thr = 0.f;      /* threKadaneT^2 */
+    float mask_thr = 0.f;      /* threMask (IQR units) */
     /* dedispersion launch shapes */
     int s1_var = 0;   /* resident stage-1 launch shape, 0 = default */
     int s2_kb = 36;   /* stage-2 shared memory per CTA, KB (36: six CTAs per SM) */
@@ -77,6 +80,16 @@ void launch_zero_rows(float *x, long ldx, const int32_t *rows, int nrows, long N
                       cudaStream_t st);
 void launch_kadane(float *x, long ldx, int C, long N, int tdk, int fdk, float thr,
                    long wnlimit, float *ds, int32_t *ranges, cudaStream_t st);
+/* kadaneT: maximum-sum band along frequency per downsampled sample; ranges [Nds][4]
+ * (channel start,end of the positive and negative band, -1 if not zapped). */
+void launch_kadaneT(float *x, long ldx, int C, long N, int tdk, int fdk, float thr,
+                    long bwlimit, float *ds, int32_t *ranges, cudaStream_t st);
+/* mask: pixels of the td x fd downsampled block outside [Q1 - t*R, Q3 + t*R] are zapped;
+ * sel: device scratch of MASK_SEL_WORDS words (selection state, then Q1, Q3 and the two
+ * limits as float bits); nzap: device int receiving the number of zapped pixels. */
+constexpr int MASK_SEL_WORDS = 2 * 256 + 8;
+void launch_mask(float *x, long ldx, int C, long N, int tdk, int fdk, float thr, float *ds,
+                 uint32_t *sel, int32_t *nzap, cudaStream_t st);
 void launch_zdot(float *x, long ldx, int C, long N, float *s, double *sstats,
                  cudaStream_t st);
 /* x16: FP16 copy of the channel buffer (same layout, used by the 16-bit precisions, may be

@@ -198,15 +198,23 @@ int plan_row(const txg_row &cfg, int nchans_raw, const double *freqs_raw, double
         if (hit) P.zap_chan.push_back(j);
     }
     P.kad_thr = cfg.threKadaneF * cfg.threKadaneF;
+    P.kadT_thr = cfg.threKadaneT * cfg.threKadaneT;
+    P.mask_thr = cfg.threMask;
+    /* channel width of the row, for the kadaneT band limit */
+    const double chbw = P.C > 1 ? std::fabs(P.freqs[1] - P.freqs[0]) : 0.;
     for (int r = 0; r < cfg.nrfi; r++) {
-        if (cfg.rfi_kind[r] == TXG_RFI_KADANEF) {
+        const int kind = cfg.rfi_kind[r];
+        if (kind == TXG_RFI_KADANEF || kind == TXG_RFI_KADANET || kind == TXG_RFI_MASK) {
             if (cfg.rfi_td[r] < 1 || cfg.rfi_fd[r] < 1) {
-                err = "kadaneF td/fd must be positive";
+                err = "kadaneF/kadaneT/mask td and fd must be positive";
                 return TXG_ERR_ARG;
             }
-            P.kad_wnlimit[r] = (long)(cfg.widthlimit / (P.tsamp * cfg.rfi_td[r]));
-        } else if (cfg.rfi_kind[r] != TXG_RFI_ZDOT) {
-            err = "unsupported rfilist entry (kadaneF and zdot are implemented)";
+            if (kind == TXG_RFI_KADANEF)
+                P.kad_wnlimit[r] = (long)(cfg.widthlimit / (P.tsamp * cfg.rfi_td[r]));
+            else if (kind == TXG_RFI_KADANET) /* minimum band in downsampled channels */
+                P.kad_wnlimit[r] = chbw > 0. ? (long)(cfg.bandlimitKT / (chbw * cfg.rfi_fd[r])) : 0;
+        } else if (kind != TXG_RFI_ZDOT && kind != TXG_RFI_ZERO) {
+            err = "unsupported rfilist entry";
             return TXG_ERR_UNSUPPORTED;
         }
     }

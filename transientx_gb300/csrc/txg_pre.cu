@@ -14,6 +14,8 @@
  */
 #include <cstdio>
 
+#include <algorithm>
+
 #include "txg_internal.h"
 
 namespace txg {
@@ -439,6 +441,142 @@ __global__ void k_kadane_apply(float *__restrict__ x, long ldx, long N, int fdk,
         x[(long)jr * ldx + i] = 0.f;
 }
 
+/* ---- kadaneT ---------------------------------------------------------------------------- */
+/* One thread per downsampled sample i runs the maximum-sum scan over its band (ds[i*Cds + j],
+ * j ascending) for the positive and the negated series, then the S/N test: the band is
+ * zapped when it spans more than bwlimit downsampled channels and snr^2 exceeds thr. */
+__global__ void k_kadaneT_scan(const float *__restrict__ ds, int Cds, long Nds, int tdk, int fdk,
+                               float thr, long bwlimit, int32_t *__restrict__ ranges)
+{
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= Nds) return;
+    const float *row = ds + i * Cds;
+    float bestp = -INFINITY, bestn = -INFINITY, curp = 0.f, curn = 0.f;
+    long csp = 0, csn = 0, sp = 0, ep = -1, sn = 0, en = -1;
+    auto step = [&](long j, float v) {
+        curp = __fadd_rn(curp, v);
+        curn = __fadd_rn(curn, -v);
+        if (curp > bestp) { bestp = curp; sp = csp; ep = j; }
+        if (curn > bestn) { bestn = curn; sn = csn; en = j; }
+        if (curp < 0.f) { curp = 0.f; csp = j + 1; }
+        if (curn < 0.f) { curn = 0.f; csn = j + 1; }
+    };
+    long j = 0;
+    for (; j + 8 <= Cds; j += 8) {
+        float v[8];
+#pragma unroll
+        for (int r = 0; r < 8; r++) v[r] = row[j + r];
+#pragma unroll
+        for (int r = 0; r < 8; r++) step(j + r, v[r]);
+    }
+    for (; j < Cds; j++) step(j, row[j]);
+    const float var = (float)(tdk * fdk);
+#pragma unroll
+    for (int p = 0; p < 2; p++) {
+        const float boxsum = p == 0 ? bestp : bestn;
+        const long s = p == 0 ? sp : sn, e = p == 0 ? ep : en;
+        const long wn = e - s + 1;
+        float snr2 = 0.f;
+        if (wn > bwlimit) snr2 = __fdiv_rn(__fmul_rn(boxsum, boxsum), __fmul_rn((float)wn, var));
+        const bool zap = Cds > 0 && snr2 > thr;
+        ranges[4 * i + 2 * p] = zap ? (int32_t)(s * fdk) : -1;
+        ranges[4 * i + 2 * p + 1] = zap ? (int32_t)((e + 1) * fdk) : -1;
+    }
+}
+
+__global__ void k_kadaneT_apply(float *__restrict__ x, long ldx, long N, int tdk, long Nds,
+                                const int32_t *__restrict__ ranges)
+{
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.y;
+    if (t >= N || t / tdk >= Nds) return;
+    const int32_t *r = ranges + 4 * (t / tdk);
+    if ((r[0] >= 0 && c >= r[0] && c < r[1]) || (r[2] >= 0 && c >= r[2] && c < r[3]))
+        x[(long)c * ldx + t] = 0.f;
+}
+
+/* ---- mask ------------------------------------------------------------------------------- */
+/* Exact order statistics of the downsampled block by radix selection on order-preserving
+ * 32-bit keys: four 8-bit passes, each a histogram of the keys that still match the selected
+ * prefix (two targets at once, Q1 and Q3) and a one-thread pick of the digit holding the
+ * remaining rank.  sel: [0,512) histograms, 512.. prefix/rank per target, 516.. results. */
+__device__ __forceinline__ uint32_t order_key(float f)
+{
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float order_key_inv(uint32_t k)
+{
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+__global__ void __launch_bounds__(256) k_mask_hist(const float *__restrict__ ds, long n,
+                                                   uint32_t *__restrict__ sel, int shift)
+{
+    __shared__ uint32_t h[512];
+    for (int b = threadIdx.x; b < 512; b += blockDim.x) h[b] = 0;
+    __syncthreads();
+    const uint32_t p0 = sel[512], p1 = sel[514];
+    const int hs = shift + 8;
+    for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+        const uint32_t k = order_key(ds[e]);
+        const uint32_t d = (k >> shift) & 255u;
+        if (hs >= 32 || (k >> hs) == (p0 >> hs)) atomicAdd(&h[d], 1u);
+        if (hs >= 32 || (k >> hs) == (p1 >> hs)) atomicAdd(&h[256 + d], 1u);
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < 512; b += blockDim.x)
+        if (h[b]) atomicAdd(&sel[b], h[b]);
+}
+
+__global__ void k_mask_pick(uint32_t *__restrict__ sel, int shift, uint32_t k0, uint32_t k1,
+                            float thr)
+{
+    if (threadIdx.x != 0) return;
+    for (int t = 0; t < 2; t++) {
+        uint32_t prefix = shift == 24 ? 0u : sel[512 + 2 * t];
+        uint32_t rank = shift == 24 ? (t == 0 ? k0 : k1) : sel[513 + 2 * t];
+        uint32_t cum = 0, digit = 255;
+        for (uint32_t b = 0; b < 256; b++) {
+            const uint32_t c = sel[256 * t + b];
+            if (rank < cum + c) {
+                digit = b;
+                break;
+            }
+            cum += c;
+        }
+        sel[512 + 2 * t] = prefix | (digit << shift);
+        sel[513 + 2 * t] = rank - cum;
+    }
+    for (int b = 0; b < 512; b++) sel[b] = 0;
+    if (shift == 0) {
+        const float q1 = order_key_inv(sel[512]), q3 = order_key_inv(sel[514]);
+        const float r = __fsub_rn(q3, q1);
+        const float lo = __fsub_rn(q1, __fmul_rn(thr, r)), hi = __fadd_rn(q3, __fmul_rn(thr, r));
+        sel[516] = __float_as_uint(q1);
+        sel[517] = __float_as_uint(q3);
+        sel[518] = __float_as_uint(lo);
+        sel[519] = __float_as_uint(hi);
+    }
+}
+
+__global__ void k_mask_apply(float *__restrict__ x, long ldx, long N, int Cds, long Nds, int tdk,
+                             int fdk, const float *__restrict__ ds, const uint32_t *__restrict__ sel,
+                             int32_t *__restrict__ nzap)
+{
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.y;
+    const long i = t / tdk;
+    const int j = c / fdk;
+    if (t >= N || i >= Nds || j >= Cds) return;
+    const float lo = __uint_as_float(sel[518]), hi = __uint_as_float(sel[519]);
+    const float d = ds[i * Cds + j];
+    if (d < lo || d > hi) {
+        x[(long)c * ldx + t] = 0.f;
+        if (c % fdk == 0 && t % tdk == 0) atomicAdd(nzap, 1);
+    }
+}
+
 /* ---- zdot ------------------------------------------------------------------------------ */
 __global__ void __launch_bounds__(256) k_zdot_norm(float *__restrict__ x, long ldx, int C, long N)
 {
@@ -589,6 +727,41 @@ void launch_kadane(float *x, long ldx, int C, long N, int tdk, int fdk, float th
     k_kadane_scan<<<nblk(Cds, 64), 64, 0, st>>>(ds, Cds, Nds, tdk, fdk, thr, wnlimit, ranges);
     dim3 g3(nblk(N, 256), Cds * fdk);
     k_kadane_apply<<<g3, 256, 0, st>>>(x, ldx, N, fdk, ranges);
+}
+
+void launch_kadaneT(float *x, long ldx, int C, long N, int tdk, int fdk, float thr,
+                    long bwlimit, float *ds, int32_t *ranges, cudaStream_t st)
+{
+    const int Cds = C / fdk;
+    const long Nds = N / tdk;
+    if (Cds <= 0 || Nds <= 0) return;
+    dim3 g1(nblk(Nds, 128), Cds);
+    k_kadane_ds<<<g1, 128, 0, st>>>(x, ldx, Cds, Nds, tdk, fdk, ds);
+    k_kadaneT_scan<<<nblk(Nds, 64), 64, 0, st>>>(ds, Cds, Nds, tdk, fdk, thr, bwlimit, ranges);
+    dim3 g3(nblk(N, 256), Cds * fdk);
+    k_kadaneT_apply<<<g3, 256, 0, st>>>(x, ldx, N, tdk, Nds, ranges);
+}
+
+void launch_mask(float *x, long ldx, int C, long N, int tdk, int fdk, float thr, float *ds,
+                 uint32_t *sel, int32_t *nzap, cudaStream_t st)
+{
+    const int Cds = C / fdk;
+    const long Nds = N / tdk;
+    cudaMemsetAsync(nzap, 0, sizeof(int32_t), st);
+    if (Cds <= 0 || Nds <= 0) return;
+    const long n = (long)Cds * Nds;
+    dim3 g1(nblk(Nds, 128), Cds);
+    k_kadane_ds<<<g1, 128, 0, st>>>(x, ldx, Cds, Nds, tdk, fdk, ds);
+    cudaMemsetAsync(sel, 0, sizeof(uint32_t) * MASK_SEL_WORDS, st);
+    /* ranks of the quartiles, as the channel zap takes them: sorted[n/4], sorted[n-1-n/4] */
+    const uint32_t k0 = (uint32_t)(n / 4), k1 = (uint32_t)(n - 1 - n / 4);
+    const unsigned hb = (unsigned)std::min<long>(nblk(n, 256), 152L * 8);
+    for (int shift = 24; shift >= 0; shift -= 8) {
+        k_mask_hist<<<hb, 256, 0, st>>>(ds, n, sel, shift);
+        k_mask_pick<<<1, 32, 0, st>>>(sel, shift, k0, k1, thr);
+    }
+    dim3 g3(nblk(N, 256), Cds * fdk);
+    k_mask_apply<<<g3, 256, 0, st>>>(x, ldx, N, Cds, Nds, tdk, fdk, ds, sel, nzap);
 }
 
 void launch_zdot(float *x, long ldx, int C, long N, float *s, double *sstats, cudaStream_t st)
