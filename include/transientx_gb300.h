@@ -178,6 +178,20 @@ int txg_get_block(txg_handle *h, int32_t beam, int32_t row, float *out);
 int txg_get_zap_ranges(txg_handle *h, int32_t beam, int32_t row, int32_t irfi, int32_t *out,
                        int64_t cap);
 
+/* SubbandDedispersion::get_subdata(sub, idm, true) (candplot.cpp:123) of the row's last
+ * block: the nsub subband series of fine DM idm aligned at that DM, [nsub][nsamples], each the
+ * sum of its subband's channels (txg_get_tables' sub_start gives the counts).  Valid after
+ * txg_sync when that block was gated; TXG_ERR_STATE otherwise. */
+int txg_get_subdata(txg_handle *h, int32_t beam, int32_t row, int64_t idm, float *out);
+
+/* The frequency band of each candidate, the fl and fh columns of the .cands line
+ * (candplot.cpp:143-231,423-433): per subband the sum over samples (isamp-wn, isamp+wn) of its
+ * channel mean, the maximum-sum run of subbands, and fl/fh = the run's ends on the linear
+ * axis from the first to the last subband's mean frequency.  Same validity as
+ * txg_get_subdata. */
+int txg_cand_band(txg_handle *h, int32_t beam, int32_t row, const txg_cand *c, int64_t n,
+                  float *fl, float *fh);
+
 /* Channels zapped by the skewness/kurtosis filter in the last block of a beam: mask[c] = 1
  * (nchans raw channels). */
 int txg_get_mask(txg_handle *h, int32_t beam, uint8_t *mask);

@@ -14,7 +14,9 @@
 #ifndef TRANSIENTX_GB300_HPP
 #define TRANSIENTX_GB300_HPP
 
+#include <algorithm>
 #include <cctype>
+#include <cstdio>
 #include <sstream>
 #include <stdexcept>
 #include <string>
@@ -160,6 +162,59 @@ inline std::vector<SinglePulse> parse_ddplan(const std::string &text, SinglePuls
     return rows;
 }
 
+/* The .cands lines of CandPlot::plot (candplot.cpp:32-433): one per reported candidate of a
+ * block, descending S/N (stable), columns beam, running number, MJD, DM, width (ms), S/N,
+ * fl, fh, plot name, row id, input file name.  The plot is not produced. */
+class CandsWriter {
+public:
+    CandsWriter(std::string rootname, double tstart, std::string beam = "0", std::string fname = "")
+        : root_(std::move(rootname)), beam_(std::move(beam)), fname_(std::move(fname)), tstart_(tstart)
+    {
+    }
+    /* <rootname>_<tstart, 10 decimals>_<beam>.cands (candplot.cpp:420) */
+    std::string filename() const { return root_ + "_" + fixed(tstart_, 10) + "_" + beam_ + ".cands"; }
+
+    std::vector<std::string> format_block(const std::vector<txg_cand> &c, long counter, long offset,
+                                          long ndump, double tsamp, double dms, double ddm,
+                                          const std::vector<float> &fl, const std::vector<float> &fh,
+                                          int row_id)
+    {
+        std::vector<size_t> idx(c.size());
+        for (size_t k = 0; k < idx.size(); k++) idx[k] = k;
+        std::stable_sort(idx.begin(), idx.end(), [&](size_t a, size_t b) { return c[a].S > c[b].S; });
+        char sid[16];
+        snprintf(sid, sizeof(sid), "%02d", row_id);
+        const double bmjd = tstart_ + (-offset + counter - ndump) * tsamp / 86400.;
+        std::vector<std::string> lines;
+        for (size_t i = 0; i < idx.size(); i++) {
+            const txg_cand &x = c[idx[i]];
+            const double mjd = tstart_ + (-offset + counter - ndump + (long)x.isamp) * tsamp / 86400.;
+            char sk[16];
+            snprintf(sk, sizeof(sk), "%02d", (int)(i + 1));
+            const std::string base = root_ + "_" + fixed(bmjd, 10) + "_" + beam_ + "_" + sk + "_" + sid;
+            std::ostringstream o;
+            o << beam_ << "\t" << ++num_cand_ << "\t" << fixed(mjd, 15) << "\t"
+              << fixed(dms + (long)x.idm * ddm, 2) << "\t" << fixed(x.wn * tsamp * 1000, 2) << "\t"
+              << fixed(x.S, 1) << "\t" << fixed(fl[idx[i]], 0) << "\t" << fixed(fh[idx[i]], 0) << "\t"
+              << base << ".png\t" << sid << "\t" << fname_ << "\n";
+            lines.push_back(o.str());
+        }
+        return lines;
+    }
+    long count() const { return num_cand_; }
+
+private:
+    static std::string fixed(double v, int prec)
+    {
+        char b[64];
+        snprintf(b, sizeof(b), "%.*f", prec, v);
+        return b;
+    }
+    std::string root_, beam_, fname_;
+    double tstart_;
+    long num_cand_ = 0;
+};
+
 class Search {
 public:
     Search(const std::vector<SinglePulse> &rows, int nchans, double tsamp,
@@ -229,6 +284,16 @@ public:
         std::vector<std::tuple<long, long, int, float>> list;
         for (int64_t k = 0; k < n; k++) list.emplace_back(out[k].idm, out[k].isamp, out[k].wn, out[k].S);
         return list;
+    }
+
+    /* fl, fh of each candidate of the row's last block (for CandsWriter) */
+    void band(int row, const std::vector<txg_cand> &c, std::vector<float> &fl, std::vector<float> &fh,
+              int beam = 0) const
+    {
+        fl.assign(c.size(), 0.f);
+        fh.assign(c.size(), 0.f);
+        check(txg_cand_band(h_, beam, row, c.data(), (int64_t)c.size(), fl.data(), fh.data()),
+              "txg_cand_band");
     }
 
     txg_handle *handle() const { return h_; }

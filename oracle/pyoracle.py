@@ -146,6 +146,12 @@ def lib() -> C.CDLL:
     L.txo_mask.restype = C.c_int
     L.txo_mask.argtypes = [f32p, C.c_int, C.c_long, C.c_long, C.c_int, C.c_int, C.c_float, f32p]
     L.txo_zero.argtypes = [f32p, C.c_int, C.c_long, C.c_long, C.c_void_p]
+    L.txo_sp_dedisp.restype = C.c_void_p
+    L.txo_sp_dedisp.argtypes = [C.c_void_p]
+    L.txo_dedisp_subdata.restype = C.c_int
+    L.txo_dedisp_subdata.argtypes = [C.c_void_p, C.c_long, f32p]
+    L.txo_cand_band.argtypes = [f32p, C.c_int, C.c_long, i32p, f64p, C.c_long, C.c_int,
+                                C.POINTER(C.c_float), C.POINTER(C.c_float)]
     L.txo_boxcar_match.argtypes = [f32p, C.c_long, i32p, C.c_int, C.c_int, C.c_int, f32p, i32p]
     L.txo_boxcar_run.argtypes = [f32p, C.c_long, C.c_long, i32p, C.c_int, C.c_int, C.c_int,
                                  f32p, i32p]
@@ -294,6 +300,15 @@ def zero(x, live=None):
     return x
 
 
+def cand_band(sub, sub_start, fsub, isamp, wn):
+    """fl, fh of one candidate from the [nsub][nout] subband sums of its DM."""
+    sub = np.ascontiguousarray(sub, np.float32)
+    fl, fh = C.c_float(), C.c_float()
+    lib().txo_cand_band(sub, sub.shape[0], sub.shape[1], np.ascontiguousarray(sub_start, np.int32),
+                        np.ascontiguousarray(fsub, np.float64), isamp, wn, C.byref(fl), C.byref(fh))
+    return np.float32(fl.value), np.float32(fh.value)
+
+
 def zdot(x):
     x = np.array(x, np.float32, order="C", copy=True)
     lib().txo_zdot(x, x.shape[0], x.shape[1], x.shape[1])
@@ -411,6 +426,12 @@ class SinglePulseRow:
         if not p:
             return None
         return np.ctypeslib.as_array(p, shape=(nrows.value, 4)).copy()
+
+    def subdata(self, idm):
+        i = self.info()
+        out = np.zeros((i.nsub, i.nout), np.float32)
+        assert lib().txo_dedisp_subdata(lib().txo_sp_dedisp(self.h), idm, out) == 0
+        return out
 
     def timdata(self):
         i = self.info()

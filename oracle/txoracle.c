@@ -1034,6 +1034,51 @@ int txo_dedisp_run(txo_dedisp *dd, const float *x, long ldx)
 
 const float *txo_dedisp_timdata(const txo_dedisp *dd) { return dd->tim; }
 
+/* SubbandDedispersion::get_subdata(sub, idm, true) (candplot.cpp:123) after a gated block:
+ * the nsub subband series of fine DM idm aligned at that DM, out[s*nout + i] =
+ * ring[g][s][t0 + i + d2[idm][s]], the sums of each subband's channels (FP32 ring). */
+int txo_dedisp_subdata(const txo_dedisp *dd, long idm, float *out)
+{
+    const txo_dedisp_info *in = &dd->info;
+    if (idm < 0 || idm >= in->ndm || !dd->ring) return -1;
+    const long N = in->ndump, R = in->ring, nout = in->nout;
+    const long t0 = in->counter - N - in->offset;
+    const int nsub = in->nsub;
+    const long g = idm / in->group;
+    for (int s = 0; s < nsub; s++) {
+        const float *row = dd->ring + ((size_t)g * nsub + s) * R;
+        const int32_t d = dd->d2[(size_t)idm * nsub + s];
+        for (long i = 0; i < nout; i++) out[(size_t)s * nout + i] = row[pmod(t0 + i + d, R)];
+    }
+    return 0;
+}
+
+/* The fl/fh of a candidate's .cands line (candplot.cpp:143-231): per subband j the sum over
+ * samples i in (isamp-wn, isamp+wn) of sub[j][i]/fcnt[j] (ascending i, from 0), the
+ * maximum-sum run of subbands (txo_kadane), and fl, fh = the ends of that run on the linear
+ * frequency axis vfnorm[j] = f[0] + j/(nsub-1.)*(f[nsub-1] - f[0]) of the subband
+ * frequencies f (here the mean frequency of each subband's channels). */
+void txo_cand_band(const float *sub, int nsub, long nout, const int32_t *sub_start,
+                   const double *fsub, long isamp, int wn, float *fl, float *fh)
+{
+    float *vpf = (float *)malloc(sizeof(float) * nsub);
+    const long lo = isamp - wn + 1 < 0 ? 0 : isamp - wn + 1;
+    const long hi = isamp + wn < nout ? isamp + wn : nout;
+    for (int j = 0; j < nsub; j++) {
+        const float cnt = (float)(sub_start[j + 1] - sub_start[j]);
+        float acc = 0.f;
+        for (long i = lo; i < hi; i++) acc = acc + sub[(size_t)j * nout + i] / cnt;
+        vpf[j] = acc;
+    }
+    long fs = 0, fe = 0;
+    txo_kadane(vpf, nsub, &fs, &fe);
+    if (fe < 0) fe = 0;
+    const double den = nsub > 1 ? nsub - 1. : 1.;
+    *fl = (float)(fsub[0] + fs / den * (fsub[nsub - 1] - fsub[0]));
+    *fh = (float)(fsub[0] + fe / den * (fsub[nsub - 1] - fsub[0]));
+    free(vpf);
+}
+
 /* ---------------------------------------------------------------------------------------
  * One ddplan row: SinglePulse::prepare/run (singlepulse.cpp:206-254, 287-341) without the
  * plotting; the rfilist ops run in their listed order.
@@ -1180,6 +1225,7 @@ const int32_t *txo_sp_zap_ranges(const txo_sp *sp, int irfi, int *nrows)
 }
 
 const float *txo_sp_timdata(const txo_sp *sp) { return sp->dd->tim; }
+const txo_dedisp *txo_sp_dedisp(const txo_sp *sp) { return sp->dd; }
 const uint8_t *txo_sp_mask(const txo_sp *sp) { return sp->mask; }
 const float *txo_sp_mxS(const txo_sp *sp) { return sp->mxS; }
 const int *txo_sp_mxwn(const txo_sp *sp) { return sp->mxwn; }

@@ -98,6 +98,9 @@ int txo_dedisp_run(txo_dedisp *dd, const float *x, long ldx);
 const float *txo_dedisp_timdata(const txo_dedisp *dd);
 void txo_dedisp_set_fp64(txo_dedisp *dd);
 const double *txo_dedisp_timdata64(const txo_dedisp *dd);
+int txo_dedisp_subdata(const txo_dedisp *dd, long idm, float *out);
+void txo_cand_band(const float *sub, int nsub, long nout, const int32_t *sub_start,
+                   const double *fsub, long isamp, int wn, float *fl, float *fh);
 
 /* ---- one ddplan row, the SinglePulse::run chain --------------------------------------- */
 enum { TXO_RFI_KADANEF = 1, TXO_RFI_ZDOT = 2, TXO_RFI_MASK = 3, TXO_RFI_KADANET = 4, TXO_RFI_ZERO = 5 };
@@ -138,6 +141,7 @@ const uint8_t *txo_sp_mask(const txo_sp *sp);
 const float *txo_sp_mxS(const txo_sp *sp);
 const int *txo_sp_mxwn(const txo_sp *sp);
 void txo_sp_freqs(const txo_sp *sp, double *out);
+const txo_dedisp *txo_sp_dedisp(const txo_sp *sp);
 
 void txo_set_threads(int n);
 

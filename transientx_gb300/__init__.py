@@ -86,6 +86,7 @@ EXPORTS = [
     "txg_get_block", "txg_get_zap_ranges", "txg_get_tables", "txg_width_ladder", "txg_boxcar",
     "txg_cluster", "txg_get_timing", "txg_get_stream", "txg_strerror", "txg_version",
     "txg_describe_row", "txg_pop_result", "txg_get_mask", "txg_kadaneF_noalloc",
+    "txg_get_subdata", "txg_cand_band",
 ]
 
 _lib: Optional[C.CDLL] = None
@@ -127,6 +128,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.txg_get_timing.argtypes = [vp, vp, vp, C.c_int32]
     L.txg_get_stream.argtypes = [vp, C.POINTER(vp)]
     L.txg_get_mask.argtypes = [vp, C.c_int32, vp]
+    L.txg_get_subdata.argtypes = [vp, C.c_int32, C.c_int32, C.c_int64, vp]
+    L.txg_cand_band.argtypes = [vp, C.c_int32, C.c_int32, vp, C.c_int64, vp, vp]
     L.txg_kadaneF_noalloc.argtypes = [vp, C.c_int64, C.c_int32, C.c_int64, C.c_int32, C.c_int32,
                                       C.c_float, C.c_int64, vp, vp]
     L.txg_pop_result.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(txg_result), vp, C.c_int64,
@@ -400,6 +403,22 @@ class Search:
         _check(load_library().txg_get_timdata(self.h, beam, row, idm0, count, _ptr(out)),
                "timdata")
         return out
+
+    def subdata(self, idm: int, row: int = 0, beam: int = 0) -> np.ndarray:
+        """SubbandDedispersion::get_subdata of the last block: [nsub][nsamples] subband sums."""
+        i = self.row_info(row, beam)
+        out = np.zeros((i.nsub, i.nsamples), np.float32)
+        _check(load_library().txg_get_subdata(self.h, beam, row, idm, _ptr(out)), "subdata")
+        return out
+
+    def cand_band(self, cands: np.ndarray, row: int = 0, beam: int = 0):
+        """fl, fh of the .cands line for each candidate (idm, isamp, wn, S) of the last block."""
+        c = np.ascontiguousarray(cands, CAND_DTYPE)
+        fl = np.zeros(len(c), np.float32)
+        fh = np.zeros(len(c), np.float32)
+        _check(load_library().txg_cand_band(self.h, beam, row, _ptr(c), len(c), _ptr(fl),
+                                            _ptr(fh)), "cand_band")
+        return fl, fh
 
     def block(self, row: int = 0, beam: int = 0) -> np.ndarray:
         i = self.row_info(row, beam)

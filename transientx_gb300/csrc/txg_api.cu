@@ -14,6 +14,7 @@
  * second stream, overlapping the previous block's kernels.
  */
 #include <algorithm>
+#include <cmath>
 #include <condition_variable>
 #include <cstdio>
 #include <cstdlib>
@@ -977,6 +978,95 @@ int txg_get_zap_ranges(txg_handle *h, int32_t beam, int32_t row, int32_t irfi, i
     TXG_CUDA_TRY(cudaStreamSynchronize(h->st));
     TXG_CUDA_TRY(cudaMemcpy(out, h->br[beam][row].ranges[irfi], 4 * rows * sizeof(int32_t),
                             cudaMemcpyDeviceToHost));
+    return TXG_OK;
+}
+
+/* The subband ring holds the last block's output window only while that block is the row's
+ * newest: every pushed block harvested (txg_sync) and the block gated. */
+static int last_block_window(txg_handle *h, int32_t beam, int32_t row, long *t0_mod)
+{
+    int rc = check_beam_row(h, beam, row);
+    if (rc) return rc;
+    const RowPlan &P = h->rp[row];
+    const BeamRow &b = h->br[beam][row];
+    for (const Slot &sl : b.slot)
+        if (sl.pending) return fail(TXG_ERR_STATE, "call txg_sync first");
+    if (!b.gated) return fail(TXG_ERR_STATE, "the row's last block produced no output");
+    *t0_mod = pmod(b.counter - P.N - P.offset, P.R);
+    return TXG_OK;
+}
+
+int txg_get_subdata(txg_handle *h, int32_t beam, int32_t row, int64_t idm, float *out)
+{
+    long t0_mod = 0;
+    int rc = last_block_window(h, beam, row, &t0_mod);
+    if (rc) return rc;
+    const RowPlan &P = h->rp[row];
+    if (!out || idm < 0 || idm >= P.cfg.ndm) return fail(TXG_ERR_ARG, "DM index or output");
+    const size_t cnt = (size_t)P.nsub * P.nout;
+    float *d = nullptr;
+    TXG_CUDA_TRY(cudaMalloc(&d, cnt * sizeof(float)));
+    launch_subdata(h->br[beam][row].ring, P.R, P.nsub, P.G, h->rd[row].d2, idm, t0_mod, P.nout,
+                   h->prec, d, h->st);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    if (e == cudaSuccess) e = cudaMemcpy(out, d, cnt * sizeof(float), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return set_cuda_error(e, "txg_get_subdata", __FILE__, __LINE__);
+    return TXG_OK;
+}
+
+int txg_cand_band(txg_handle *h, int32_t beam, int32_t row, const txg_cand *c, int64_t n,
+                  float *fl, float *fh)
+{
+    long t0_mod = 0;
+    int rc = last_block_window(h, beam, row, &t0_mod);
+    if (rc) return rc;
+    if (n <= 0) return TXG_OK;
+    if (!c || !fl || !fh) return fail(TXG_ERR_ARG, "null argument");
+    const RowPlan &P = h->rp[row];
+    for (long k = 0; k < n; k++)
+        if (c[k].idm < 0 || c[k].idm >= P.cfg.ndm || c[k].wn < 1)
+            return fail(TXG_ERR_ARG, "candidate outside the row");
+    std::vector<float> vpf((size_t)n * P.nsub);
+    txg_cand *dc = nullptr;
+    float *dv = nullptr;
+    cudaError_t e = cudaMalloc(&dc, n * sizeof(txg_cand));
+    if (e == cudaSuccess) e = cudaMalloc(&dv, vpf.size() * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dc, c, n * sizeof(txg_cand), cudaMemcpyHostToDevice, h->st);
+    if (e == cudaSuccess) {
+        launch_cand_vpf(h->br[beam][row].ring, P.R, P.nsub, P.G, h->rd[row].d2, h->rd[row].sub_start,
+                        t0_mod, P.nout, dc, n, h->prec, dv, h->st);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    if (e == cudaSuccess) e = cudaMemcpy(vpf.data(), dv, vpf.size() * sizeof(float), cudaMemcpyDeviceToHost);
+    cudaFree(dc);
+    cudaFree(dv);
+    if (e != cudaSuccess) return set_cuda_error(e, "txg_cand_band", __FILE__, __LINE__);
+    /* the maximum-sum run of subbands (strictly larger sum wins, restart below zero) and its
+     * ends on the linear frequency axis of candplot.cpp:151 */
+    const double den = P.nsub > 1 ? P.nsub - 1. : 1.;
+    const double f0 = P.fsub.front(), f1 = P.fsub.back();
+    for (long k = 0; k < n; k++) {
+        const float *v = vpf.data() + (size_t)k * P.nsub;
+        float best = -INFINITY, cur = 0.f;
+        long cs = 0, fs = 0, fe = 0;
+        for (long j = 0; j < P.nsub; j++) {
+            cur = cur + v[j];
+            if (cur > best) {
+                best = cur;
+                fs = cs;
+                fe = j;
+            }
+            if (cur < 0.f) {
+                cur = 0.f;
+                cs = j + 1;
+            }
+        }
+        fl[k] = (float)(f0 + fs / den * (f1 - f0));
+        fh[k] = (float)(f0 + fe / den * (f1 - f0));
+    }
     return TXG_OK;
 }
 

@@ -853,6 +853,75 @@ long stage2_span(const int32_t *d2h, int nsub, int G, long ndm)
     return span;
 }
 
+/* ---- subband series of one DM (get_subdata) and candidate bands ------------------------ */
+template <typename T>
+__global__ void k_subdata(const T *__restrict__ ring, long R, int nsub, int G, const int32_t *__restrict__ d2,
+                          long k, long t0_mod, long nout, float *__restrict__ out)
+{
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = blockIdx.y;
+    if (i >= nout) return;
+    const long g = k / G;
+    const long t = (t0_mod + i + d2[(size_t)k * nsub + s]) % R;
+    out[(size_t)s * nout + i] = to_f(ring[((size_t)g * nsub + s) * R + t]);
+}
+
+/* One CTA per candidate: per subband, the sum over samples (isamp-wn, isamp+wn) of the
+ * subband sample divided by its channel count, ascending from 0.0f. */
+template <typename T>
+__global__ void k_cand_vpf(const T *__restrict__ ring, long R, int nsub, int G,
+                           const int32_t *__restrict__ d2, const int32_t *__restrict__ sub_start,
+                           long t0_mod, long nout, const txg_cand *__restrict__ c,
+                           float *__restrict__ vpf)
+{
+    const txg_cand cd = c[blockIdx.x];
+    const long k = cd.idm, g = k / G;
+    const long lo = max(0L, (long)cd.isamp - cd.wn + 1), hi = min(nout, (long)cd.isamp + cd.wn);
+    for (int s = threadIdx.x; s < nsub; s += blockDim.x) {
+        const float cnt = (float)(sub_start[s + 1] - sub_start[s]);
+        const T *row = ring + ((size_t)g * nsub + s) * R;
+        const long d = d2[(size_t)k * nsub + s];
+        float acc = 0.f;
+        for (long i = lo; i < hi; i++) acc = __fadd_rn(acc, __fdiv_rn(to_f(row[(t0_mod + i + d) % R]), cnt));
+        vpf[(size_t)blockIdx.x * nsub + s] = acc;
+    }
+}
+
+template <typename T>
+static void subdata_impl(const void *ring, long R, int nsub, int G, const int32_t *d2, long k,
+                         long t0_mod, long nout, float *out, cudaStream_t st)
+{
+    dim3 grid(nblk(nout, 256), nsub);
+    k_subdata<T><<<grid, 256, 0, st>>>((const T *)ring, R, nsub, G, d2, k, t0_mod, nout, out);
+}
+
+void launch_subdata(const void *ring, long R, int nsub, int G, const int32_t *d2, long k,
+                    long t0_mod, long nout, int prec, float *out, cudaStream_t st)
+{
+    if (prec == TXG_PREC_BF16)
+        subdata_impl<__nv_bfloat16>(ring, R, nsub, G, d2, k, t0_mod, nout, out, st);
+    else if (prec == TXG_PREC_FP16)
+        subdata_impl<__half>(ring, R, nsub, G, d2, k, t0_mod, nout, out, st);
+    else
+        subdata_impl<float>(ring, R, nsub, G, d2, k, t0_mod, nout, out, st);
+}
+
+void launch_cand_vpf(const void *ring, long R, int nsub, int G, const int32_t *d2,
+                     const int32_t *sub_start, long t0_mod, long nout, const txg_cand *c, long n,
+                     int prec, float *vpf, cudaStream_t st)
+{
+    if (n <= 0) return;
+    if (prec == TXG_PREC_BF16)
+        k_cand_vpf<__nv_bfloat16><<<(unsigned)n, 128, 0, st>>>((const __nv_bfloat16 *)ring, R, nsub, G, d2,
+                                                               sub_start, t0_mod, nout, c, vpf);
+    else if (prec == TXG_PREC_FP16)
+        k_cand_vpf<__half><<<(unsigned)n, 128, 0, st>>>((const __half *)ring, R, nsub, G, d2, sub_start,
+                                                        t0_mod, nout, c, vpf);
+    else
+        k_cand_vpf<float><<<(unsigned)n, 128, 0, st>>>((const float *)ring, R, nsub, G, d2, sub_start,
+                                                       t0_mod, nout, c, vpf);
+}
+
 /* Ring length a stage-2 window may need (the ring must be longer, so a window wraps once). */
 long stage2_window(long span) { return (long)S2_TT + span + 16; }
 

@@ -34,6 +34,7 @@ struct RowPlan {
     long ldh = 0;         /* row stride of the channel buffer */
     std::vector<int32_t> sub_start; /* nsub+1 */
     std::vector<double> fref;       /* nsub */
+    std::vector<double> fsub;       /* nsub: mean frequency of each subband's channels */
     std::vector<int32_t> d1;        /* [ng][C] */
     std::vector<int32_t> d2;        /* [ndm][nsub] */
     std::vector<int32_t> vwn;
@@ -105,6 +106,13 @@ long stage2_window(long span);
 void launch_stage2(const void *ring, long R, int nsub, int G, long ndm, long nout,
                    const int32_t *d2, long span, long t0_mod, int prec, int s2_kb, float *tim,
                    long ldt, int *err, cudaStream_t st);
+/* the subband series of fine DM k ([nsub][nout] floats) and, per candidate, the per-subband
+ * sums over its window (vpf [n][nsub]) from the subband ring */
+void launch_subdata(const void *ring, long R, int nsub, int G, const int32_t *d2, long k,
+                    long t0_mod, long nout, int prec, float *out, cudaStream_t st);
+void launch_cand_vpf(const void *ring, long R, int nsub, int G, const int32_t *d2,
+                     const int32_t *sub_start, long t0_mod, long nout, const txg_cand *c, long n,
+                     int prec, float *vpf, cudaStream_t st);
 int launch_boxcar(const float *tim, long ldt, long ndm, long n, const int32_t *vwn, int nw,
                   int iqr, int avx2_tail, float thre, txg_cand *cand, int *ncand, long cap,
                   float *mxS, int32_t *mxwn, int *err, cudaStream_t st);

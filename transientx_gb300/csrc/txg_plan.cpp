@@ -144,6 +144,12 @@ int plan_row(const txg_row &cfg, int nchans_raw, const double *freqs_raw, double
     P.ng = (int)((ndm + P.G - 1) / P.G);
     std::vector<double> flow;
     subbands(P.C, P.nsub, P.freqs, P.sub_start, P.fref, flow);
+    P.fsub.assign(P.nsub, 0.);
+    for (int s = 0; s < P.nsub; s++) {
+        double acc = 0.;
+        for (int j = P.sub_start[s]; j < P.sub_start[s + 1]; j++) acc += P.freqs[j];
+        P.fsub[s] = acc / (double)(P.sub_start[s + 1] - P.sub_start[s]);
+    }
     P.d1.assign((size_t)P.ng * P.C, 0);
     P.d2.assign((size_t)ndm * P.nsub, 0);
     P.maxd1 = 0;
