@@ -59,3 +59,44 @@ def test_boxcar_rejects_bad_arguments(tx):
     with pytest.raises(tx.TxgError) as e:
         tx.boxcar(np.zeros((2, 10), np.float32), [])
     assert e.value.status == tx.ERR_ARG
+
+
+@pytest.mark.parametrize("n", [62496, 100003])
+def test_boxcar_long_rows_vs_oracle(tx, oracle, n):
+    """Rows longer than one CTA's shared memory (16 us sampling, 1 s blocks) run on the
+    segmented kernels: same agreement with the oracle as short rows."""
+    rng = np.random.default_rng(n)
+    ndm = 5
+    tim = rng.normal(0, 20, (ndm, n)).astype(np.float32)
+    tim[0, n // 3: n // 3 + 40] += 200
+    tim[2, n - 30:] += 400   # near the row end, inside the last segment's halo
+    tim[4] = 2.0             # var = 0 row
+    vwn = oracle.width_ladder(1e-4, 0.01, 0.1, 16e-6)
+    for iqr in (False, True):
+        for avx in (False, True):
+            Sr, Wr = oracle.boxcar_run(tim, vwn, iqr, avx)
+            S, W, c = tx.boxcar(tim, vwn, iqr=iqr, avx2_tail=avx, thre=5.0)
+            assert_boxcar_close(tim, vwn, S, W, Sr, Wr, iqr=iqr)
+            assert_cands_close(c, oracle.threshold_scan(Sr, Wr, 5.0), 5.0)
+
+
+@pytest.mark.parametrize("n", [1000, 15625, 40000])
+def test_boxcar_segmented_equals_single_cta(tx, oracle, n, monkeypatch):
+    """The segmented kernels rebuild the single-CTA kernel's running sum chunk by chunk, so on
+    rows that fit both they give bit-identical S, widths and candidates."""
+    rng = np.random.default_rng(n + 1)
+    tim = rng.normal(0, 20, (9, n)).astype(np.float32)
+    tim[1, n // 2: n // 2 + 9] += 250
+    vwn = oracle.width_ladder(1e-4, 0.05, 0.1, 64e-6)
+    vwn = vwn[vwn < max(3, n // 2)]
+    for iqr in (False, True):
+        for avx in (False, True):
+            monkeypatch.delenv("TXG_BOXCAR_SEGMENTED", raising=False)
+            S1, W1, c1 = tx.boxcar(tim, vwn, iqr=iqr, avx2_tail=avx, thre=4.0)
+            monkeypatch.setenv("TXG_BOXCAR_SEGMENTED", "1")
+            S2, W2, c2 = tx.boxcar(tim, vwn, iqr=iqr, avx2_tail=avx, thre=4.0)
+            monkeypatch.delenv("TXG_BOXCAR_SEGMENTED")
+            np.testing.assert_array_equal(S1, S2)
+            np.testing.assert_array_equal(W1, W2)
+            np.testing.assert_array_equal(np.sort(c1, order=["idm", "isamp"]),
+                                          np.sort(c2, order=["idm", "isamp"]))

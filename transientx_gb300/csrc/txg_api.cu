@@ -178,6 +178,7 @@ struct BeamRow {
     uint8_t *live = nullptr;
     void *ring = nullptr;
     float *tim = nullptr;
+    double *bx_scratch = nullptr; /* boxcar statistics and chunk offsets of long rows */
     float *mxS = nullptr;
     int32_t *mxwn = nullptr;
     Slot slot[NSLOT];
@@ -522,9 +523,10 @@ int run_block(txg_handle *h, int beam, const uint8_t *raw)
                           pmod(t0, P.R), h->prec, P.s2_kb, b.tim, P.nout, sl.dcount + 1, h->st);
             TXG_CUDA_TRY(cudaGetLastError());
             if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[4], h->st));
-            rc = launch_boxcar(b.tim, P.nout, P.cfg.ndm, P.nout, D.vwn, (int)P.vwn.size(),
+            rc = launch_boxcar(b.tim, P.nout, P.cfg.ndm, P.nout, D.vwn, (int)P.vwn.size(), P.maxwn,
                                P.cfg.iqr, (h->flags & TXG_FLAG_AVX2_TAIL) ? 1 : 0, P.cfg.thre,
-                               sl.dcand, sl.dcount, h->cap, b.mxS, b.mxwn, sl.dcount + 1, h->st);
+                               sl.dcand, sl.dcount, h->cap, b.mxS, b.mxwn, b.bx_scratch,
+                               sl.dcount + 1, h->st);
             if (rc) return rc;
             TXG_CUDA_TRY(cudaGetLastError());
             if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[5], h->st));
@@ -580,11 +582,11 @@ int finish_plan(RowPlan &P, int r)
         if (const char *q = strstr(e, "s1=")) P.s1_var = (sscanf(q + 3, "%d", &v) == 1) ? v : P.s1_var;
         if (const char *q = strstr(e, "s2kb=")) P.s2_kb = (sscanf(q + 5, "%d", &v) == 1 && v >= 16 && v <= 200) ? v : P.s2_kb;
     }
-    if ((size_t)P.nout > boxcar_max_samples())
-        return fail(TXG_ERR_UNSUPPORTED, "row " + std::to_string(r) +
-                                             ": ndump+noverlap exceeds the boxcar row limit of " +
-                                             std::to_string(boxcar_max_samples()) + " samples");
     if (P.vwn.size() > 256) return fail(TXG_ERR_UNSUPPORTED, "more than 256 boxcar widths");
+    if (!boxcar_supported(P.nout, P.maxwn, (int)P.vwn.size()))
+        return fail(TXG_ERR_UNSUPPORTED, "row " + std::to_string(r) +
+                                             ": ndump+noverlap or the widest boxcar exceeds the "
+                                             "boxcar kernels' limits");
     return TXG_OK;
 }
 
@@ -765,6 +767,7 @@ int txg_create(const txg_plan *plan, txg_handle **out)
             if ((rc = dalloc(h, &ring, (size_t)P.ng * P.nsub * P.R * ring_elem(h->prec)))) return bail(rc);
             b.ring = ring;
             if ((rc = dalloc(h, &b.tim, (size_t)P.cfg.ndm * P.nout))) return bail(rc);
+            if ((rc = dalloc(h, &b.bx_scratch, boxcar_scratch_doubles(P.cfg.ndm)))) return bail(rc);
             if (h->flags & TXG_FLAG_DENSE) {
                 if ((rc = dalloc(h, &b.mxS, (size_t)P.cfg.ndm * P.nout)) ||
                     (rc = dalloc(h, &b.mxwn, (size_t)P.cfg.ndm * P.nout)))
@@ -1126,8 +1129,10 @@ int txg_boxcar(const float *tim, int64_t ndm, int64_t nsamples, const int32_t *v
 {
     if (!tim || !vwn || ndm < 1 || nsamples < 1 || nw < 1 || nw > 256)
         return fail(TXG_ERR_ARG, "need tim, vwn, ndm >= 1, nsamples >= 1, 1 <= nw <= 256");
-    if ((size_t)nsamples > boxcar_max_samples())
-        return fail(TXG_ERR_UNSUPPORTED, "nsamples exceeds the boxcar row limit");
+    int maxwn = 0;
+    for (int w = 0; w < nw; w++) maxwn = std::max(maxwn, (int)vwn[w]);
+    if (!boxcar_supported(nsamples, maxwn, nw))
+        return fail(TXG_ERR_UNSUPPORTED, "nsamples or the widest boxcar exceeds the boxcar kernels' limits");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return fail(TXG_ERR_NODEVICE, "no CUDA device");
     cudaStream_t st;
@@ -1136,6 +1141,7 @@ int txg_boxcar(const float *tim, int64_t ndm, int64_t nsamples, const int32_t *v
     int32_t *dwn = nullptr, *dvwn = nullptr;
     txg_cand *dc = nullptr;
     int *dcount = nullptr;
+    double *dscr = nullptr;
     const size_t cnt = (size_t)ndm * nsamples;
     const long ccap = cands ? (cap > 0 ? cap : 0) : 0;
     int rc = TXG_OK;
@@ -1147,6 +1153,7 @@ int txg_boxcar(const float *tim, int64_t ndm, int64_t nsamples, const int32_t *v
         cudaFree(dvwn);
         cudaFree(dc);
         cudaFree(dcount);
+        cudaFree(dscr);
         cudaStreamDestroy(st);
     };
     do {
@@ -1154,6 +1161,7 @@ int txg_boxcar(const float *tim, int64_t ndm, int64_t nsamples, const int32_t *v
         if ((e = cudaMalloc(&dtim, cnt * sizeof(float))) != cudaSuccess ||
             (e = cudaMalloc(&dvwn, nw * sizeof(int32_t))) != cudaSuccess ||
             (e = cudaMalloc(&dcount, 2 * sizeof(int))) != cudaSuccess ||
+            (e = cudaMalloc(&dscr, boxcar_scratch_doubles(ndm) * sizeof(double))) != cudaSuccess ||
             (e = cudaMalloc(&dc, (ccap > 0 ? ccap : 1) * sizeof(txg_cand))) != cudaSuccess ||
             (mxS && (e = cudaMalloc(&dS, cnt * sizeof(float))) != cudaSuccess) ||
             (mxS && (e = cudaMalloc(&dwn, cnt * sizeof(int32_t))) != cudaSuccess)) {
@@ -1166,8 +1174,9 @@ int txg_boxcar(const float *tim, int64_t ndm, int64_t nsamples, const int32_t *v
             rc = set_cuda_error(e, "copy-in", __FILE__, __LINE__);
             break;
         }
-        rc = launch_boxcar(dtim, nsamples, ndm, nsamples, dvwn, nw, iqr, (flags & TXG_FLAG_AVX2_TAIL) ? 1 : 0,
-                           thre, dc, dcount, ccap, dS, dwn, dcount + 1, st);
+        rc = launch_boxcar(dtim, nsamples, ndm, nsamples, dvwn, nw, maxwn, iqr,
+                           (flags & TXG_FLAG_AVX2_TAIL) ? 1 : 0, thre, dc, dcount, ccap, dS, dwn,
+                           dscr, dcount + 1, st);
         if (rc) break;
         if ((e = cudaGetLastError()) != cudaSuccess) {
             rc = set_cuda_error(e, "boxcar launch", __FILE__, __LINE__);

@@ -14,6 +14,7 @@
  */
 #include <algorithm>
 #include <cfloat>
+#include <cstdlib>
 
 #include "txg_internal.h"
 
@@ -95,18 +96,19 @@ __device__ float select_kth(const float *row, long n, long k, unsigned *hist)
  * per-width range test (needed near the row ends); AVX2 reproduces the unordered-compare blend
  * of the -mavx2 build. */
 template <bool CHECK, bool AVX2>
-__device__ __forceinline__ void widths_pass(const float *__restrict__ c, int i0, int n, int nw,
-                                            const int4 *__restrict__ wpar,
+__device__ __forceinline__ void widths_pass(const float *__restrict__ c, int coff, int i0, int iend,
+                                            int nw, const int4 *__restrict__ wpar,
                                             const float *__restrict__ temp_w, float *best, int *bw)
 {
+    /* c[j - coff] holds the running sum at sample j; samples at or past iend are skipped */
     for (int w = 0; w < nw; w++) {
         const int4 p = wpar[w];
         const float tw = temp_w[w];
 #pragma unroll
         for (int u = 0; u < BX_U; u++) {
             const int i = i0 + u * BX_THREADS;
-            if (!CHECK || (i >= p.x && i < p.z)) {
-                const float S = __fmul_rn(__fsub_rn(c[i + p.y], c[i - p.x]), tw);
+            if (!CHECK || (i >= p.x && i < p.z && i < iend)) {
+                const float S = __fmul_rn(__fsub_rn(c[i - coff + p.y], c[i - coff - p.x]), tw);
                 if (S >= best[u]) {
                     best[u] = S;
                     bw[u] = p.w;
@@ -254,9 +256,9 @@ k_boxcar(const float *__restrict__ tim, long ldt, long n, const int32_t *__restr
         if (active) {
             const int i0 = base + tid;
             if (base >= lo_all && base + BX_THREADS * BX_U <= hi_all)
-                widths_pass<false, AVX2>(c, i0, nn, nw, wpar, temp_w, best, bw);
+                widths_pass<false, AVX2>(c, 0, i0, nn, nw, wpar, temp_w, best, bw);
             else
-                widths_pass<true, AVX2>(c, i0, nn, nw, wpar, temp_w, best, bw);
+                widths_pass<true, AVX2>(c, 0, i0, nn, nw, wpar, temp_w, best, bw);
         }
 #pragma unroll
         for (int u = 0; u < BX_U; u++) {
@@ -280,26 +282,257 @@ k_boxcar(const float *__restrict__ tim, long ldt, long n, const int32_t *__restr
     }
 }
 
+/* ---- rows longer than one CTA's shared memory ------------------------------------------ */
+/* The single-CTA kernel's arithmetic depends only on n: statistics by the fixed run pattern,
+ * and the running sum over BX_THREADS chunks of L = ceil(n/BX_THREADS) samples (FP32 inside a
+ * chunk, FP64 chunk offsets).  k_boxcar_prep computes, per row, the same statistics and chunk
+ * offsets from global memory; k_boxcar_seg rebuilds the running sum of a segment of chunks
+ * plus a halo of the widest boxcar and runs the same width passes: results are identical to
+ * k_boxcar's.  scratch row k: [0, BX_THREADS) chunk offsets, [BX_THREADS] mean and var. */
+constexpr int SEG_CHUNKS = 32; /* chunks per segment CTA */
+
+__global__ void __launch_bounds__(BX_THREADS)
+k_boxcar_prep(const float *__restrict__ tim, long ldt, long n, int iqr, double *__restrict__ scratch)
+{
+    __shared__ double red[BX_THREADS / 32];
+    __shared__ double chunk_off[BX_THREADS];
+    __shared__ unsigned hist[256];
+    __shared__ float mean_sh, var_sh;
+    const long k = blockIdx.x;
+    const int tid = threadIdx.x;
+    const float *row = tim + k * ldt;
+    if (!iqr) {
+        double s1 = 0., s2 = 0.;
+        long i = tid;
+        while (i < n) {
+            float r1 = 0.f, r2 = 0.f;
+            for (int r = 0; r < 8 && i < n; r++, i += BX_THREADS) {
+                float v = row[i];
+                r1 = __fadd_rn(r1, v);
+                r2 = __fadd_rn(r2, __fmul_rn(v, v));
+            }
+            s1 = __dadd_rn(s1, (double)r1);
+            s2 = __dadd_rn(s2, (double)r2);
+        }
+        s1 = block_sum_d(s1, red);
+        s2 = block_sum_d(s2, red);
+        if (tid == 0) {
+            double m = __ddiv_rn(s1, (double)n);
+            double v = __dsub_rn(__ddiv_rn(s2, (double)n), __dmul_rn(m, m));
+            mean_sh = __double2float_rn(m);
+            var_sh = __double2float_rn(v);
+        }
+    } else {
+        float q1 = select_kth(row, n, n / 4, hist);
+        float q2 = select_kth(row, n, n / 2, hist);
+        float q3 = select_kth(row, n, n - 1 - n / 4, hist);
+        if (tid == 0) {
+            double d = __ddiv_rn((double)__fsub_rn(q3, q1), 1.349);
+            mean_sh = q2;
+            var_sh = __double2float_rn(__dmul_rn(d, d));
+        }
+    }
+    __syncthreads();
+    const float mean = mean_sh;
+    const long L = (n + BX_THREADS - 1) / BX_THREADS;
+    const long a = (long)tid * L, b = a + L < n ? a + L : n;
+    float loc = 0.f;
+    for (long i = a; i < b; i++) loc = __fadd_rn(loc, __fsub_rn(row[i], mean));
+    chunk_off[tid] = (double)loc;
+    __syncthreads();
+    if (tid < 32) {
+        const int per = BX_THREADS / 32;
+        double v[BX_THREADS / 32];
+        double run = 0.;
+#pragma unroll
+        for (int q = 0; q < per; q++) {
+            v[q] = chunk_off[tid * per + q];
+            run = __dadd_rn(run, v[q]);
+        }
+        double incl = run;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            double y = __shfl_up_sync(FULL, incl, off);
+            if (tid >= off) incl = __dadd_rn(incl, y);
+        }
+        const double left = __shfl_up_sync(FULL, incl, 1);
+        double ex = tid == 0 ? 0. : left;
+#pragma unroll
+        for (int q = 0; q < per; q++) {
+            chunk_off[tid * per + q] = ex;
+            ex = __dadd_rn(ex, v[q]);
+        }
+    }
+    __syncthreads();
+    double *out = scratch + k * (BX_THREADS + 1);
+    out[tid] = chunk_off[tid];
+    if (tid == 0) {
+        float *mv = reinterpret_cast<float *>(out + BX_THREADS);
+        mv[0] = mean_sh;
+        mv[1] = var_sh;
+    }
+}
+
+template <bool AVX2>
+__global__ void __launch_bounds__(BX_THREADS)
+k_boxcar_seg(const float *__restrict__ tim, long ldt, long n, const int32_t *__restrict__ vwn,
+             int nw, float thre, const double *__restrict__ scratch, txg_cand *__restrict__ cand,
+             int *__restrict__ ncand, long cap, float *__restrict__ mxS, int32_t *__restrict__ mxwn)
+{
+    const int avx2_tail = AVX2 ? 1 : 0;
+    extern __shared__ __align__(16) float c[];
+    __shared__ float temp_w[256];
+    __shared__ int4 wpar[256];
+    __shared__ int lo_all, hi_all, wlmax_sh, whmax_sh;
+    const long k = blockIdx.x;
+    const int tid = threadIdx.x;
+    const float *row = tim + k * ldt;
+    const double *sc = scratch + k * (BX_THREADS + 1);
+    const float mean = reinterpret_cast<const float *>(sc + BX_THREADS)[0];
+    const float var = reinterpret_cast<const float *>(sc + BX_THREADS)[1];
+    const long L = (n + BX_THREADS - 1) / BX_THREADS;
+    const long s_lo = (long)blockIdx.y * SEG_CHUNKS * L;
+    if (s_lo >= n) return;
+    const long s_hi = min(n, s_lo + (long)SEG_CHUNKS * L);
+
+    for (int w = tid; w < nw; w += BX_THREADS) {
+        const int wn = vwn[w];
+        const int wl = wn / 2 + 1, wh = (wn - 1) / 2;
+        temp_w[w] = __double2float_rn(__dsqrt_rn(__ddiv_rn(1., (double)__fmul_rn((float)wn, var))));
+        long hi = n - wh;
+        if (avx2_tail) {
+            long len = n - wh - wl;
+            long nv = len >= 0 ? len / 8 : 0;
+            hi = nv > 0 ? wl + 8 * nv : wl;
+        }
+        wpar[w] = make_int4(wl, wh, (int)hi, wn);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        int lo = 0, hi = (int)n, wl = 0, wh = 0;
+        for (int w = 0; w < nw; w++) {
+            lo = max(lo, wpar[w].x);
+            hi = min(hi, wpar[w].z);
+            wl = max(wl, wpar[w].x);
+            wh = max(wh, wpar[w].y);
+        }
+        lo_all = lo;
+        hi_all = hi;
+        wlmax_sh = wl;
+        whmax_sh = wh;
+    }
+    __syncthreads();
+    /* running sum over the segment and its halo, rebuilt chunk by chunk from the offsets */
+    const long h_lo = max(0L, s_lo - wlmax_sh), h_hi = min(n, s_hi + whmax_sh);
+    for (long ch = h_lo / L + tid; ch <= (h_hi - 1) / L; ch += BX_THREADS) {
+        const long a = ch * L, b = min(a + L, n);
+        const double off = sc[ch];
+        float run = 0.f;
+        for (long i = a; i < b; i++) {
+            run = __fadd_rn(run, __fsub_rn(row[i], mean));
+            if (i >= h_lo && i < h_hi) c[i - h_lo] = __double2float_rn(__dadd_rn(off, (double)run));
+        }
+    }
+    __syncthreads();
+
+    const bool active = var > 0.f;
+    const int lane = tid & 31;
+    const int coff = (int)h_lo, iend = (int)s_hi;
+    for (int base = (int)s_lo; base < iend; base += BX_THREADS * BX_U) {
+        float best[BX_U];
+        int bw[BX_U];
+#pragma unroll
+        for (int u = 0; u < BX_U; u++) {
+            best[u] = 0.f;
+            bw[u] = 0;
+        }
+        if (active) {
+            const int i0 = base + tid;
+            if (base >= lo_all && base + BX_THREADS * BX_U <= hi_all && base + BX_THREADS * BX_U <= iend)
+                widths_pass<false, AVX2>(c, coff, i0, iend, nw, wpar, temp_w, best, bw);
+            else
+                widths_pass<true, AVX2>(c, coff, i0, iend, nw, wpar, temp_w, best, bw);
+        }
+#pragma unroll
+        for (int u = 0; u < BX_U; u++) {
+            const int i = base + tid + u * BX_THREADS;
+            if (i < iend && mxS) {
+                mxS[k * n + i] = best[u];
+                mxwn[k * n + i] = bw[u];
+            }
+            const bool hit = i < iend && best[u] > thre;
+            const unsigned m = __ballot_sync(FULL, hit);
+            if (m) {
+                int basei = 0;
+                if (lane == __ffs(m) - 1) basei = atomicAdd(ncand, __popc(m));
+                basei = __shfl_sync(FULL, basei, __ffs(m) - 1);
+                if (hit) {
+                    const long slot = basei + __popc(m & ((1u << lane) - 1u));
+                    if (slot < cap) cand[slot] = txg_cand{(int32_t)k, (int32_t)i, bw[u], best[u]};
+                }
+            }
+        }
+    }
+}
+
 } // namespace
 
 size_t boxcar_max_samples() { return (BX_SMEM_MAX) / sizeof(float); }
 
+size_t boxcar_scratch_doubles(long ndm) { return (size_t)ndm * (BX_THREADS + 1); }
+
+bool boxcar_supported(long n, int maxwn, int nw)
+{
+    if (n <= 0 || n >= (1L << 31) || nw > 256) return false;
+    if ((size_t)n <= boxcar_max_samples()) return true;
+    const long L = (n + BX_THREADS - 1) / BX_THREADS;
+    const long seg = (long)SEG_CHUNKS * L;
+    return (size_t)(seg + maxwn + 2) * sizeof(float) <= BX_SMEM_MAX && (n + seg - 1) / seg <= 65535;
+}
+
+static bool force_segmented()
+{
+    const char *e = getenv("TXG_BOXCAR_SEGMENTED");
+    return e && e[0] == '1';
+}
+
 int launch_boxcar(const float *tim, long ldt, long ndm, long n, const int32_t *vwn, int nw,
-                  int iqr, int avx2_tail, float thre, txg_cand *cand, int *ncand, long cap,
-                  float *mxS, int32_t *mxwn, int *err, cudaStream_t st)
+                  int maxwn, int iqr, int avx2_tail, float thre, txg_cand *cand, int *ncand,
+                  long cap, float *mxS, int32_t *mxwn, double *scratch, int *err, cudaStream_t st)
 {
     (void)err;
     if (n <= 0 || ndm <= 0) return TXG_OK;
-    if ((size_t)n > boxcar_max_samples() || nw > 256) return TXG_ERR_UNSUPPORTED;
-    size_t smem = (size_t)n * sizeof(float);
+    if (nw > 256 || n >= (1L << 31)) return TXG_ERR_UNSUPPORTED;
+    if ((size_t)n <= boxcar_max_samples() && !(force_segmented() && scratch)) {
+        size_t smem = (size_t)n * sizeof(float);
+        if (avx2_tail) {
+            cudaFuncSetAttribute(k_boxcar<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BX_SMEM_MAX);
+            k_boxcar<true><<<(unsigned)ndm, BX_THREADS, smem, st>>>(tim, ldt, n, vwn, nw, iqr, thre, cand,
+                                                                    ncand, cap, mxS, mxwn);
+        } else {
+            cudaFuncSetAttribute(k_boxcar<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BX_SMEM_MAX);
+            k_boxcar<false><<<(unsigned)ndm, BX_THREADS, smem, st>>>(tim, ldt, n, vwn, nw, iqr, thre, cand,
+                                                                     ncand, cap, mxS, mxwn);
+        }
+        return TXG_OK;
+    }
+    /* long rows: statistics and chunk offsets per row, then segments of SEG_CHUNKS chunks */
+    if (!scratch) return TXG_ERR_UNSUPPORTED;
+    const long L = (n + BX_THREADS - 1) / BX_THREADS;
+    const long seg = (long)SEG_CHUNKS * L;
+    const long nseg = (n + seg - 1) / seg;
+    const size_t smem = (size_t)(seg + maxwn + 2) * sizeof(float);
+    if (smem > BX_SMEM_MAX || nseg > 65535) return TXG_ERR_UNSUPPORTED;
+    k_boxcar_prep<<<(unsigned)ndm, BX_THREADS, 0, st>>>(tim, ldt, n, iqr, scratch);
+    dim3 grid((unsigned)ndm, (unsigned)nseg);
     if (avx2_tail) {
-        cudaFuncSetAttribute(k_boxcar<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BX_SMEM_MAX);
-        k_boxcar<true><<<(unsigned)ndm, BX_THREADS, smem, st>>>(tim, ldt, n, vwn, nw, iqr, thre, cand,
-                                                                ncand, cap, mxS, mxwn);
+        cudaFuncSetAttribute(k_boxcar_seg<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_boxcar_seg<true><<<grid, BX_THREADS, smem, st>>>(tim, ldt, n, vwn, nw, thre, scratch, cand,
+                                                           ncand, cap, mxS, mxwn);
     } else {
-        cudaFuncSetAttribute(k_boxcar<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BX_SMEM_MAX);
-        k_boxcar<false><<<(unsigned)ndm, BX_THREADS, smem, st>>>(tim, ldt, n, vwn, nw, iqr, thre, cand,
-                                                                 ncand, cap, mxS, mxwn);
+        cudaFuncSetAttribute(k_boxcar_seg<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_boxcar_seg<false><<<grid, BX_THREADS, smem, st>>>(tim, ldt, n, vwn, nw, thre, scratch, cand,
+                                                            ncand, cap, mxS, mxwn);
     }
     return TXG_OK;
 }

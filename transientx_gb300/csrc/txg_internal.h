@@ -113,9 +113,13 @@ void launch_subdata(const void *ring, long R, int nsub, int G, const int32_t *d2
 void launch_cand_vpf(const void *ring, long R, int nsub, int G, const int32_t *d2,
                      const int32_t *sub_start, long t0_mod, long nout, const txg_cand *c, long n,
                      int prec, float *vpf, cudaStream_t st);
+/* Boxcar::run on [ndm][n] series.  Rows longer than boxcar_max_samples() use the segmented
+ * kernels and need scratch (boxcar_scratch_doubles(ndm) doubles); maxwn bounds the halo. */
+size_t boxcar_scratch_doubles(long ndm);
+bool boxcar_supported(long n, int maxwn, int nw);
 int launch_boxcar(const float *tim, long ldt, long ndm, long n, const int32_t *vwn, int nw,
-                  int iqr, int avx2_tail, float thre, txg_cand *cand, int *ncand, long cap,
-                  float *mxS, int32_t *mxwn, int *err, cudaStream_t st);
+                  int maxwn, int iqr, int avx2_tail, float thre, txg_cand *cand, int *ncand,
+                  long cap, float *mxS, int32_t *mxwn, double *scratch, int *err, cudaStream_t st);
 size_t boxcar_max_samples();
 
 } // namespace txg
