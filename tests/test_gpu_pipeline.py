@@ -119,6 +119,36 @@ def test_rfi_options_match_oracle(tx, oracle, name):
             assert fired.get(op[0], 0) > 0, (name, op, fired)
 
 
+def test_beams_of_one_handle_equal_separate_handles(tx):
+    """nbeams > 1: each beam keeps its own history, ring and candidates; two beams of one
+    handle give exactly what two one-beam handles give (beams pushed interleaved)."""
+    from transientx_gb300 import synth
+    fil, rows, ndump = small_workload()
+    fil2 = synth.Filterbank(fil.nchans, fil.tsamp, fil.freqs, fil.nsamples, 99,
+                            pulses=[(0.4 * fil.nsamples * fil.tsamp, 120.0, 2e-3, 30.0)])
+    flags = tx.FLAG_KEEP_SERIES | tx.FLAG_DENSE
+    with tx.Search(rows, fil.nchans, fil.tsamp, fil.freqs, ndump, nbeams=2, flags=flags) as m, \
+            tx.Search(rows, fil.nchans, fil.tsamp, fil.freqs, ndump, flags=flags) as a, \
+            tx.Search(rows, fil.nchans, fil.tsamp, fil.freqs, ndump, flags=flags) as b:
+        ngated = 0
+        for blk in range(fil.nsamples // ndump):
+            r0, r1 = fil.generate(blk * ndump, ndump), fil2.generate(blk * ndump, ndump)
+            m.push_block(r0, beam=0)
+            m.push_block(r1, beam=1)
+            a.push_block(r0)
+            b.push_block(r1)
+            m.sync(), a.sync(), b.sync()
+            for r in range(len(rows)):
+                for beam, single in ((0, a), (1, b)):
+                    assert m.row_info(r, beam).gated == single.row_info(r).gated
+                    np.testing.assert_array_equal(m.block(r, beam), single.block(r))
+                    if single.row_info(r).gated:
+                        ngated += 1
+                        np.testing.assert_array_equal(m.timdata(r, beam), single.timdata(r))
+                        np.testing.assert_array_equal(m.candidates(r, beam), single.candidates(r))
+        assert ngated > 0
+
+
 def test_skzap_catches_sinusoids(tx, oracle):
     fil, rows, ndump = small_workload()
     sines = sorted(c for c, _, _, _ in fil.sines)

@@ -467,7 +467,9 @@ int run_block(txg_handle *h, int beam, const uint8_t *raw)
         if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[0], h->st));
 
         /* history: the last H columns of the previous block go in front of this one */
-        float *xprev = b.xh[b.cur ^ 1], *xcur = b.xh[b.cur];
+        /* one buffer when the history is shorter than a block (the previous block's last H
+         * columns [N, N+H) move to [0, H), stream-ordered after its stage 1); two otherwise */
+        float *xprev = b.xh[1] ? b.xh[b.cur ^ 1] : b.xh[0], *xcur = b.xh[1] ? b.xh[b.cur] : b.xh[0];
         if (P.H > 0)
             TXG_CUDA_TRY(cudaMemcpy2DAsync(xcur, P.ldh * sizeof(float), xprev + P.N,
                                            P.ldh * sizeof(float), P.H * sizeof(float), P.C,
@@ -558,7 +560,7 @@ int run_block(txg_handle *h, int beam, const uint8_t *raw)
         sl.counter = counter;
         b.pushed = counter;
         b.nblocks++;
-        b.cur ^= 1;
+        if (b.xh[1]) b.cur ^= 1;
     }
     return status;
 }
@@ -742,7 +744,7 @@ int txg_create(const txg_plan *plan, txg_handle **out)
         for (int r = 0; r < plan->nrows; r++) {
             RowPlan &P = h->rp[r];
             BeamRow &b = h->br[beam][r];
-            for (int i = 0; i < 2; i++)
+            for (int i = 0; i < (P.N >= P.H ? 1 : 2); i++)
                 if ((rc = dalloc(h, &b.xh[i], (size_t)P.C * P.ldh))) return bail(rc);
             if (h->prec != TXG_PREC_FP32 && (rc = dalloc(h, &b.x16, (size_t)P.C * P.ldh))) return bail(rc);
             long kmax = 1;
@@ -953,7 +955,7 @@ int txg_get_block(txg_handle *h, int32_t beam, int32_t row, float *out)
     const BeamRow &b = h->br[beam][row];
     if (b.nblocks == 0) return fail(TXG_ERR_STATE, "no block pushed");
     TXG_CUDA_TRY(cudaStreamSynchronize(h->st));
-    const float *x = b.xh[b.cur ^ 1] + P.H; /* buffer of the newest block */
+    const float *x = (b.xh[1] ? b.xh[b.cur ^ 1] : b.xh[0]) + P.H; /* buffer of the newest block */
     TXG_CUDA_TRY(cudaMemcpy2D(out, P.N * sizeof(float), x, P.ldh * sizeof(float), P.N * sizeof(float), P.C,
                               cudaMemcpyDeviceToHost));
     return TXG_OK;
