@@ -119,6 +119,28 @@ def test_rfi_options_match_oracle(tx, oracle, name):
             assert fired.get(op[0], 0) > 0, (name, op, fired)
 
 
+@pytest.mark.parametrize("nchans,td,fd", [(128, 1, 1), (128, 3, 2), (256, 2, 16), (100, 2, 5),
+                                          (96, 4, 3)])
+def test_unpack_paths_match_oracle(tx, oracle, nchans, td, fd):
+    """Unpack + downsample: the 16-byte path (channels a multiple of 16, fd dividing 16) and
+    the staged fallback give the oracle's preprocessed block exactly, with the channel zap."""
+    from transientx_gb300 import SinglePulse, synth
+    ndump = 1536 * td
+    f = synth.band(nchans, 1500.0, 1200.0)
+    fil = synth.Filterbank(nchans, 256e-6, f, 3 * ndump, 7,
+                           sines=[(5, 25.0, 0.03, 0.0), (nchans - 3, 30.0, 0.01, 1.0)])
+    rows = [SinglePulse(td=td, fd=fd, dms=0.0, ddm=1.0, ndm=16, maxw=0.02, bswidth=0.0)]
+    orow = oracle_rows(oracle, rows, fil, ndump, tx, zapthre=3.0)[0]
+    with tx.Search(rows, nchans, fil.tsamp, f, ndump, flags=tx.FLAG_KEEP_SERIES, zapthre=3.0) as s:
+        for blk in range(3):
+            raw = fil.generate(blk * ndump, ndump)
+            s.push_block(raw)
+            s.sync()
+            orow.run(raw)
+            np.testing.assert_array_equal(s.mask(), orow.mask())
+            np.testing.assert_array_equal(s.block(0), orow.block(), err_msg=f"block {blk}")
+
+
 def test_beams_of_one_handle_equal_separate_handles(tx):
     """nbeams > 1: each beam keeps its own history, ring and candidates; two beams of one
     handle give exactly what two one-beam handles give (beams pushed interleaved)."""

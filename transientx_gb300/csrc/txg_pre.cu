@@ -253,6 +253,61 @@ __global__ void __launch_bounds__(256) k_unpack(const uint8_t *__restrict__ raw,
     }
 }
 
+/* Unpack for fd | 16 and 16-byte rows: each thread sums, for one output sample, the td raw
+ * rows of one 16-channel group (one 16-byte load per row; 16/fd output channels), and a
+ * shared-memory transpose gives channel-major coalesced writes.  The sums are of integers
+ * below 2^24, exact in FP32, so they equal k_unpack's in any order. */
+constexpr int UV_BYTES = 128;  /* raw bytes (channels) per CTA row: 8 groups of 16 */
+constexpr int UV_TI = 64;      /* output samples per CTA */
+
+template <int FD>
+__global__ void __launch_bounds__(256) k_unpack_vec(const uint8_t *__restrict__ raw, int C_raw,
+                                                   long n0, int td, float *__restrict__ x, long ldx,
+                                                   int C, long N, const uint8_t *__restrict__ mask)
+{
+    constexpr int TJ = UV_BYTES / FD; /* output channels per CTA */
+    constexpr int PER = 16 / FD;      /* output channels per thread */
+    __shared__ float outt[TJ][UV_TI + 1];
+    const int q = threadIdx.x & 7, srow = threadIdx.x >> 3; /* 16-byte group, sample slot 0..31 */
+    const int c0 = blockIdx.y * UV_BYTES + 16 * q;         /* first raw channel of the group */
+    const long i0 = (long)blockIdx.x * UV_TI;
+    uint4 mk = make_uint4(0u, 0u, 0u, 0u);
+    const bool in_c = c0 < C_raw;
+    if (mask && in_c) mk = *reinterpret_cast<const uint4 *>(mask + c0);
+    const uint32_t mw[4] = {mk.x, mk.y, mk.z, mk.w};
+#pragma unroll
+    for (int pass = 0; pass < UV_TI / 32; pass++) {
+        const int ii = pass * 32 + srow;
+        const long i = i0 + ii;
+        float acc[PER];
+#pragma unroll
+        for (int o = 0; o < PER; o++) acc[o] = 0.f;
+        if (in_c && i < N) {
+            const uint8_t *src = raw + (i * td) * (long)C_raw + c0;
+            for (int t = 0; t < td; t++) {
+                const uint4 v = *reinterpret_cast<const uint4 *>(src + (long)t * C_raw);
+                const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                for (int b = 0; b < 16; b++) {
+                    const uint32_t byte = (w[b >> 2] >> (8 * (b & 3))) & 255u;
+                    const uint32_t m = (mw[b >> 2] >> (8 * (b & 3))) & 255u;
+                    acc[b / FD] = __fadd_rn(acc[b / FD], m ? 0.f : (float)byte);
+                }
+            }
+        }
+#pragma unroll
+        for (int o = 0; o < PER; o++) outt[q * PER + o][ii] = acc[o];
+    }
+    __syncthreads();
+    const int j0 = blockIdx.y * TJ;
+    for (int e = threadIdx.x; e < TJ * UV_TI; e += blockDim.x) {
+        const int jj = e / UV_TI, ii = e % UV_TI;
+        const int j = j0 + jj;
+        const long i = i0 + ii;
+        if (j < C && i < N) x[(long)j * ldx + i] = outt[jj][ii];
+    }
+}
+
 /* fallback for large td*fd: one thread per output, no staging */
 __global__ void k_unpack_direct(const uint8_t *__restrict__ raw, int C_raw, int td, int fd,
                                 float *__restrict__ x, long ldx, int C, long N,
@@ -668,6 +723,20 @@ void launch_skzap(const uint8_t *raw, int C_raw, long n0, float thr, unsigned lo
 void launch_unpack(const uint8_t *raw, int C_raw, long n0, int td, int fd, float *x, long ldx,
                    int C, long N, const uint8_t *mask, cudaStream_t st)
 {
+    const bool vec = C_raw % 16 == 0 && (reinterpret_cast<uintptr_t>(raw) & 15) == 0 &&
+                     (!mask || (reinterpret_cast<uintptr_t>(mask) & 15) == 0) &&
+                     (fd == 1 || fd == 2 || fd == 4 || fd == 8 || fd == 16);
+    if (vec) {
+        dim3 grid(nblk(N, UV_TI), nblk(C_raw, UV_BYTES));
+        switch (fd) {
+        case 1: k_unpack_vec<1><<<grid, 256, 0, st>>>(raw, C_raw, n0, td, x, ldx, C, N, mask); break;
+        case 2: k_unpack_vec<2><<<grid, 256, 0, st>>>(raw, C_raw, n0, td, x, ldx, C, N, mask); break;
+        case 4: k_unpack_vec<4><<<grid, 256, 0, st>>>(raw, C_raw, n0, td, x, ldx, C, N, mask); break;
+        case 8: k_unpack_vec<8><<<grid, 256, 0, st>>>(raw, C_raw, n0, td, x, ldx, C, N, mask); break;
+        default: k_unpack_vec<16><<<grid, 256, 0, st>>>(raw, C_raw, n0, td, x, ldx, C, N, mask); break;
+        }
+        return;
+    }
     size_t smem = (size_t)UP_TI * td * UP_TJ * fd;
     if (smem <= 96 * 1024) {
         static bool attr = false;

@@ -148,4 +148,34 @@ def nchan4096_rfi(seed: int = 2, nsamples: int = 1 << 21) -> Workload:
     return Workload("nchan4096_n2M_rfi_dm3000", fil, rows, seglen_ndump(tsamp, [1, 2, 4]))
 
 
-WORKLOADS = {"nchan256_n1M_dm1000": nchan256_single, "nchan4096_n2M_rfi_dm3000": nchan4096_rfi}
+def nchan8192_dm5000(seed: int = 5, nsamples: int = 1 << 23) -> Workload:
+    """One beam of the 8192-channel survey shape: 1200-1800 MHz, 16 us, 2^23 samples (134 s),
+    RFI as the 4096-channel workload (5% sinusoid channels, zero-DM impulses at 1/s), bursts of
+    32 us-5 ms at DM 10-5000 and S/N 8-30.  Five ddplan rows to DM 5000 with td 1/2/4/8/16,
+    maxw 0.01 s, rfilist kadaneF 8 4, zdot; 1 s blocks (62496 samples at td 1)."""
+    rng = np.random.default_rng(seed)
+    tsamp, C_ = 16e-6, 8192
+    freqs = band(C_, 1800.0, 1200.0)
+    T = nsamples * tsamp
+    chans = rng.choice(C_, size=int(0.05 * C_), replace=False)
+    sines = [(int(c), float(rng.uniform(10, 30)), float(rng.uniform(2e-3, 0.2)),
+              float(rng.uniform(0, 2 * np.pi))) for c in chans]
+    nimp = rng.poisson(T)
+    imps = [(float(rng.uniform(0, T)), int(rng.integers(1, 51)), 20.0) for _ in range(nimp)]
+    pulses = [(float(t0), float(dm), float(w), float(s)) for t0, dm, w, s in zip(
+        np.sort(rng.uniform(0.05 * T, 0.9 * T, 12)), rng.uniform(10, 5000, 12),
+        np.exp(rng.uniform(np.log(32e-6), np.log(5e-3), 12)), rng.uniform(8, 30, 12))]
+    fil = Filterbank(C_, tsamp, freqs, nsamples, seed, pulses=pulses, sines=sines, impulses=imps)
+    rfi = [["kadaneF", "8", "4"], ["zdot"]]
+    rows = [
+        SinglePulse(td=1, dms=0.0, ddm=0.05, ndm=2000, maxw=0.01, rfilist=rfi, id=1),
+        SinglePulse(td=2, dms=100.0, ddm=0.1, ndm=2000, maxw=0.01, rfilist=rfi, id=2),
+        SinglePulse(td=4, dms=300.0, ddm=0.2, ndm=2000, maxw=0.01, rfilist=rfi, id=3),
+        SinglePulse(td=8, dms=700.0, ddm=0.5, ndm=2000, maxw=0.01, rfilist=rfi, id=4),
+        SinglePulse(td=16, dms=1700.0, ddm=1.0, ndm=3300, maxw=0.01, rfilist=rfi, id=5),
+    ]
+    return Workload("nchan8192_n8M_dm5000", fil, rows, seglen_ndump(tsamp, [1, 2, 4, 8, 16]))
+
+
+WORKLOADS = {"nchan256_n1M_dm1000": nchan256_single, "nchan4096_n2M_rfi_dm3000": nchan4096_rfi,
+             "nchan8192_n8M_dm5000": nchan8192_dm5000}
