@@ -38,6 +38,28 @@ __device__ __forceinline__ long long warp_sum_ll(long long v)
     return v;
 }
 
+/* r[i] = f(r[i], i) over a row by one warp, 16-byte accesses when the row is aligned (each
+ * element is independent, so the access width does not change any result). */
+template <typename F>
+__device__ __forceinline__ void row_map(float *__restrict__ r, long n, int lane, F f)
+{
+    long i0 = 0;
+    if ((reinterpret_cast<uintptr_t>(r) & 15) == 0) {
+        const long n4 = n / 4;
+        float4 *r4 = reinterpret_cast<float4 *>(r);
+        for (long q = lane; q < n4; q += 32) {
+            float4 v = r4[q];
+            v.x = f(v.x, 4 * q);
+            v.y = f(v.y, 4 * q + 1);
+            v.z = f(v.z, 4 * q + 2);
+            v.w = f(v.w, 4 * q + 3);
+            r4[q] = v;
+        }
+        i0 = 4 * n4;
+    }
+    for (long i = i0 + lane; i < n; i += 32) r[i] = f(r[i], i);
+}
+
 /* Fixed-pattern warp reduction of a row: mode 0 -> sum x, 1 -> sum x*x, 2 -> sum x*y. */
 template <int MODE>
 __device__ __forceinline__ double red32(const float *__restrict__ x, const float *__restrict__ y,
@@ -45,9 +67,22 @@ __device__ __forceinline__ double red32(const float *__restrict__ x, const float
 {
     double acc = 0.;
     long i = lane;
-    while (i < n) {
+    for (; i + 7 * 32 < n; i += 8 * 32) { /* full runs: the eight loads first */
+        float v[8];
+#pragma unroll
+        for (int r = 0; r < 8; r++) {
+            v[r] = x[i + 32 * r];
+            if (MODE == 1) v[r] = __fmul_rn(v[r], v[r]);
+            if (MODE == 2) v[r] = __fmul_rn(v[r], y[i + 32 * r]);
+        }
         float run = 0.f;
-        for (int r = 0; r < 8 && i < n; r++, i += 32) {
+#pragma unroll
+        for (int r = 0; r < 8; r++) run = __fadd_rn(run, v[r]);
+        acc = __dadd_rn(acc, (double)run);
+    }
+    if (i < n) { /* the last, partial run */
+        float run = 0.f;
+        for (; i < n; i += 32) {
             float v = x[i];
             if (MODE == 1) v = __fmul_rn(v, v);
             if (MODE == 2) v = __fmul_rn(v, y[i]);
@@ -66,9 +101,25 @@ __device__ __forceinline__ void red32x2(const float *__restrict__ x, const float
 {
     double a1 = 0., a2 = 0.;
     long i = lane;
-    while (i < n) {
+    for (; i + 7 * 32 < n; i += 8 * 32) { /* full runs: the eight loads first */
+        float v[8], q[8];
+#pragma unroll
+        for (int r = 0; r < 8; r++) {
+            v[r] = x[i + 32 * r];
+            q[r] = MODE == 1 ? v[r] : y[i + 32 * r];
+        }
         float r1 = 0.f, r2 = 0.f;
-        for (int r = 0; r < 8 && i < n; r++, i += 32) {
+#pragma unroll
+        for (int r = 0; r < 8; r++) {
+            r1 = __fadd_rn(r1, v[r]);
+            r2 = __fadd_rn(r2, __fmul_rn(v[r], q[r]));
+        }
+        a1 = __dadd_rn(a1, (double)r1);
+        a2 = __dadd_rn(a2, (double)r2);
+    }
+    if (i < n) { /* the last, partial run */
+        float r1 = 0.f, r2 = 0.f;
+        for (; i < n; i += 32) {
             const float v = x[i];
             r1 = __fadd_rn(r1, v);
             r2 = __fadd_rn(r2, MODE == 1 ? __fmul_rn(v, v) : __fmul_rn(v, y[i]));
@@ -333,8 +384,21 @@ __global__ void __launch_bounds__(256) k_equalize(float *__restrict__ x, long ld
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= C) return;
     float *r = x + (long)w * ldx;
-    long long s1 = 0, s2 = 0;
-    for (long i = lane; i < N; i += 32) {
+    long long s1 = 0, s2 = 0; /* exact integer sums: any order */
+    long i0 = 0;
+    if ((reinterpret_cast<uintptr_t>(r) & 15) == 0) {
+        const float4 *r4 = reinterpret_cast<const float4 *>(r);
+        const long n4 = N / 4;
+        for (long q = lane; q < n4; q += 32) {
+            const float4 f = r4[q];
+            const long long a = __float2ll_rn(f.x), b = __float2ll_rn(f.y), c = __float2ll_rn(f.z),
+                            d = __float2ll_rn(f.w);
+            s1 += a + b + c + d;
+            s2 += a * a + b * b + c * c + d * d;
+        }
+        i0 = 4 * n4;
+    }
+    for (long i = i0 + lane; i < N; i += 32) {
         long long v = __float2ll_rn(r[i]);
         s1 += v;
         s2 += v * v;
@@ -346,7 +410,7 @@ __global__ void __launch_bounds__(256) k_equalize(float *__restrict__ x, long ld
     double var = __dsub_rn(__ddiv_rn((double)s2, dn), __dmul_rn(mean, mean));
     double sd = var > 0. ? __dsqrt_rn(var) : 1.;
     const float mf = __double2float_rn(mean), inv = __double2float_rn(__ddiv_rn(1., sd));
-    for (long i = lane; i < N; i += 32) r[i] = __fmul_rn(__fsub_rn(r[i], mf), inv);
+    row_map(r, N, lane, [=](float v, long) { return __fmul_rn(__fsub_rn(v, mf), inv); });
     if (live && lane == 0) live[w] = var > 0. ? 1 : 0;
 }
 
@@ -411,13 +475,26 @@ __global__ void k_smooth(const float *__restrict__ z, long N, long nw, float *__
     b[i] = __fdiv_rn(acc, (float)(hi - lo + 1));
 }
 
+/* x[j][i] -= b[i] on live channels, four samples per thread (16-byte accesses when the row
+ * and b are aligned). */
 __global__ void k_sub_series(float *__restrict__ x, long ldx, long N, const float *__restrict__ b,
                              const uint8_t *__restrict__ live)
 {
-    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y;
+    const long i = 4 * ((long)blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = blockIdx.y;
     if (i >= N || (live && !live[j])) return;
-    x[(long)j * ldx + i] = __fsub_rn(x[(long)j * ldx + i], b[i]);
+    float *r = x + (long)j * ldx;
+    if (i + 3 < N && ((reinterpret_cast<uintptr_t>(r) | reinterpret_cast<uintptr_t>(b)) & 15) == 0) {
+        float4 v = *reinterpret_cast<float4 *>(r + i);
+        const float4 c = *reinterpret_cast<const float4 *>(b + i);
+        v.x = __fsub_rn(v.x, c.x);
+        v.y = __fsub_rn(v.y, c.y);
+        v.z = __fsub_rn(v.z, c.z);
+        v.w = __fsub_rn(v.w, c.w);
+        *reinterpret_cast<float4 *>(r + i) = v;
+    } else {
+        for (long k = i; k < i + 4 && k < N; k++) r[k] = __fsub_rn(r[k], b[k]);
+    }
 }
 
 __global__ void k_zero_rows(float *__restrict__ x, long ldx, const int32_t *__restrict__ rows,
@@ -645,31 +722,52 @@ __global__ void __launch_bounds__(256) k_zdot_norm(float *__restrict__ x, long l
     double var = __dsub_rn(__ddiv_rn(s2, dn), __dmul_rn(mean, mean));
     double sd = var > 0. ? __dsqrt_rn(var) : 1.;
     const float mf = __double2float_rn(mean), inv = __double2float_rn(__ddiv_rn(1., sd));
-    for (long i = lane; i < N; i += 32) r[i] = __fmul_rn(__fsub_rn(r[i], mf), inv);
+    row_map(r, N, lane, [=](float v, long) { return __fmul_rn(__fsub_rn(v, mf), inv); });
 }
 
-/* se and ss of the zero-DM series by the fixed warp pattern; the series is first staged in
- * shared memory by the whole CTA (when it fits) so the one reducing warp does not wait on
- * serialised global loads. */
-constexpr int SST_MAX = 12288; /* floats staged (48 KB) */
+/* se and ss of the zero-DM series in the fixed pattern of red32x2: lane l's runs of eight
+ * elements (l + 32*(8*rho + r)) are summed in FP32 by all threads at once, then each lane
+ * adds its run totals in FP64 in run order and the lanes combine by the xor butterfly. */
+constexpr int SST_RUNS = 4096; /* run totals staged per lane set (2 floats each) */
 
 __global__ void __launch_bounds__(1024) k_zdot_sstats(const float *__restrict__ s, long N,
                                                      double *__restrict__ out)
 {
-    __shared__ float sm[SST_MAX];
-    const bool staged = N <= SST_MAX;
-    if (staged) {
-        for (long i = threadIdx.x; i < N; i += blockDim.x) sm[i] = s[i];
+    __shared__ float run1[SST_RUNS], run2[SST_RUNS];
+    const long nruns = ((N + 31) / 32 + 7) / 8; /* runs of the longest lane */
+    double a1 = 0., a2 = 0.;
+    for (long base = 0; base < nruns; base += SST_RUNS / 32) {
+        const long nb = min((long)(SST_RUNS / 32), nruns - base);
+        for (long u = threadIdx.x; u < nb * 32; u += blockDim.x) {
+            const long rho = base + u / 32, l = u % 32;
+            float r1 = 0.f, r2 = 0.f;
+#pragma unroll
+            for (int r = 0; r < 8; r++) {
+                const long i = l + 32 * (8 * rho + r);
+                if (i < N) {
+                    const float v = s[i];
+                    r1 = __fadd_rn(r1, v);
+                    r2 = __fadd_rn(r2, __fmul_rn(v, v));
+                }
+            }
+            run1[u] = r1;
+            run2[u] = r2;
+        }
+        __syncthreads();
+        if (threadIdx.x < 32)
+            for (long q = 0; q < nb; q++) { /* an empty run is +0 and leaves the sum unchanged */
+                a1 = __dadd_rn(a1, (double)run1[q * 32 + threadIdx.x]);
+                a2 = __dadd_rn(a2, (double)run2[q * 32 + threadIdx.x]);
+            }
         __syncthreads();
     }
-    if (threadIdx.x >= 32) return;
-    const int lane = threadIdx.x;
-    const float *src = staged ? sm : s;
-    double se, ss;
-    red32x2<1>(src, nullptr, N, lane, se, ss);
-    if (lane == 0) {
-        out[0] = se;
-        out[1] = ss;
+    if (threadIdx.x < 32) {
+        a1 = warp_sum_d(a1);
+        a2 = warp_sum_d(a2);
+        if (threadIdx.x == 0) {
+            out[0] = a1;
+            out[1] = a2;
+        }
     }
 }
 
@@ -690,8 +788,7 @@ __global__ void __launch_bounds__(256) k_zdot_fit(float *__restrict__ x, long ld
         beta = __ddiv_rn(__dsub_rn(__dmul_rn(xs, se), __dmul_rn(xe, ss)), tmp);
     }
     const float af = __double2float_rn(alpha), bf = __double2float_rn(beta);
-    for (long i = lane; i < N; i += 32)
-        r[i] = __fsub_rn(r[i], __fadd_rn(__fmul_rn(af, s[i]), bf));
+    row_map(r, N, lane, [=](float v, long i) { return __fsub_rn(v, __fadd_rn(__fmul_rn(af, s[i]), bf)); });
 }
 
 inline unsigned nblk(long n, int b) { return (unsigned)((n + b - 1) / b); }
@@ -771,7 +868,7 @@ void launch_smooth(const float *z, long N, long nw, float *b, cudaStream_t st)
 void launch_sub_series(float *x, long ldx, int C, long N, const float *b, const uint8_t *live,
                        cudaStream_t st)
 {
-    dim3 grid(nblk(N, 256), C);
+    dim3 grid(nblk((N + 3) / 4, 256), C);
     k_sub_series<<<grid, 256, 0, st>>>(x, ldx, N, b, live);
 }
 
