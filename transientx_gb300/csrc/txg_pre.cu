@@ -436,12 +436,12 @@ __global__ void __launch_bounds__(32 * CSUM_BLK) k_colmean(const float *__restri
     if (i < N) {
         const float *p = x + i;
         int j = j0;
-        for (; j + 8 <= j1; j += 8) {
-            float v[8];
+        for (; j + 16 <= j1; j += 16) { /* sixteen loads in flight, added in channel order */
+            float v[16];
 #pragma unroll
-            for (int r = 0; r < 8; r++) v[r] = p[(long)(j + r) * ldx];
+            for (int r = 0; r < 16; r++) v[r] = p[(long)(j + r) * ldx];
 #pragma unroll
-            for (int r = 0; r < 8; r++) acc = __fadd_rn(acc, v[r]);
+            for (int r = 0; r < 16; r++) acc = __fadd_rn(acc, v[r]);
         }
         for (; j < j1; j++) acc = __fadd_rn(acc, p[(long)j * ldx]);
     }
@@ -524,11 +524,14 @@ __global__ void k_kadane_ds(const float *__restrict__ x, long ldx, int Cds, long
 /* One thread per downsampled channel runs the maximum-sum scan over the positive and the
  * negated series in one pass (strictly larger sum replaces the best window; the running
  * sum restarts after it drops below zero), then applies the S/N test. */
-__global__ void k_kadane_scan(const float *__restrict__ ds, int Cds, long Nds, int tdk, int fdk,
-                              float thr, long wnlimit, int32_t *__restrict__ ranges)
+constexpr int KS_T = 256; /* samples staged per tile in the kadaneF scan */
+
+__global__ void __launch_bounds__(32) k_kadane_scan(const float *__restrict__ ds, int Cds, long Nds,
+                                                    int tdk, int fdk, float thr, long wnlimit,
+                                                    int32_t *__restrict__ ranges)
 {
-    int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= Cds) return;
+    __shared__ float tile[KS_T][33];
+    const int j = blockIdx.x * 32 + threadIdx.x;
     float bestp = -INFINITY, bestn = -INFINITY, curp = 0.f, curn = 0.f;
     long csp = 0, csn = 0, sp = 0, ep = -1, sn = 0, en = -1;
     auto step = [&](long i, float v) {
@@ -539,15 +542,18 @@ __global__ void k_kadane_scan(const float *__restrict__ ds, int Cds, long Nds, i
         if (curp < 0.f) { curp = 0.f; csp = i + 1; }
         if (curn < 0.f) { curn = 0.f; csn = i + 1; }
     };
-    long i = 0;
-    for (; i + 8 <= Nds; i += 8) { /* eight loads in flight, then the sequential scan */
-        float v[8];
-#pragma unroll
-        for (int r = 0; r < 8; r++) v[r] = ds[(i + r) * Cds + j];
-#pragma unroll
-        for (int r = 0; r < 8; r++) step(i + r, v[r]);
+    /* the warp's 32 channels are staged KS_T samples at a time (coalesced rows, all loads in
+     * flight), then each lane scans its channel sequentially */
+    for (long t0 = 0; t0 < Nds; t0 += KS_T) {
+        const int nt = (int)min((long)KS_T, Nds - t0);
+#pragma unroll 16
+        for (int r = 0; r < nt; r++)
+            tile[r][threadIdx.x] = j < Cds ? ds[(t0 + r) * Cds + j] : 0.f;
+        __syncwarp();
+        for (int r = 0; r < nt; r++) step(t0 + r, tile[r][threadIdx.x]);
+        __syncwarp();
     }
-    for (; i < Nds; i++) step(i, ds[i * Cds + j]);
+    if (j >= Cds) return;
     const float var = (float)(tdk * fdk);
 #pragma unroll
     for (int p = 0; p < 2; p++) {
@@ -890,7 +896,7 @@ void launch_kadane(float *x, long ldx, int C, long N, int tdk, int fdk, float th
         dim3 g1(nblk(Nds, 128), Cds);
         k_kadane_ds<<<g1, 128, 0, st>>>(x, ldx, Cds, Nds, tdk, fdk, ds);
     }
-    k_kadane_scan<<<nblk(Cds, 64), 64, 0, st>>>(ds, Cds, Nds, tdk, fdk, thr, wnlimit, ranges);
+    k_kadane_scan<<<nblk(Cds, 32), 32, 0, st>>>(ds, Cds, Nds, tdk, fdk, thr, wnlimit, ranges);
     dim3 g3(nblk(N, 256), Cds * fdk);
     k_kadane_apply<<<g3, 256, 0, st>>>(x, ldx, N, fdk, ranges);
 }
