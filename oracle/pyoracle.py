@@ -473,6 +473,13 @@ def ref_lib(variant="scalar") -> C.CDLL:
     L.ref_boxcar_run.restype = C.c_int
     L.ref_boxcar_run.argtypes = [f32p, C.c_long, C.c_long, i32p, C.c_int, C.c_int, f32p, i32p,
                                  C.c_int]
+    L.ref_replot.restype = C.c_int
+    L.ref_replot.argtypes = [C.c_void_p, C.c_int, C.c_long, C.c_double, C.c_void_p, C.c_double,
+                             C.c_double, C.c_int, C.c_void_p, C.c_void_p, C.c_float, C.c_void_p,
+                             C.c_int, C.c_int, C.c_float, C.c_int, C.c_int, C.c_int, C.c_int,
+                             C.c_void_p, C.c_long, C.POINTER(C.c_long), C.POINTER(C.c_int),
+                             C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_double),
+                             C.POINTER(C.c_double), C.c_void_p, C.c_long, C.POINTER(C.c_int)]
     L.ref_cluster_run.restype = C.c_long
     L.ref_cluster_run.argtypes = [f32p, i32p, C.c_long, C.c_long, C.c_double, C.c_double,
                                   C.c_double, C.c_double, C.c_double, C.c_int, C.c_float,
@@ -480,6 +487,37 @@ def ref_lib(variant="scalar") -> C.CDLL:
                                   i64p, i64p, i32p, f32p, C.c_long]
     _ref[variant] = L
     return L
+
+
+def ref_replot(data, freqs, tbin, dm, width, zdot=False, kadane=None, clip=None, zapthre=3.0,
+               zap=(), fd=1, snrloss=0.1, nwidth=20, pow2bin=False, nopt=False, upto=12,
+               variant="scalar"):
+    """The reference's Candidate chain of replot_fil on one candidate ([nchan][nbin] float):
+    returns data after step `upto` (1..12) and, after step 12, snr, width, dm_maxsnr, mjd (from
+    mjd_start 0) and the S/N map."""
+    L = ref_lib(variant)
+    data = np.ascontiguousarray(data, np.float32)
+    nchan, nbin = data.shape
+    freqs = np.ascontiguousarray(freqs, np.float64)
+    out = np.zeros(nchan * nbin, np.float32)
+    nb, nc, nd = C.c_long(), C.c_int(), C.c_int()
+    snr, wid, dmx, mjd = C.c_float(), C.c_float(), C.c_double(), C.c_double()
+    smap = np.zeros(4 * nchan * nbin + 64, np.float32)
+    kad = (C.c_int * 3)(*kadane) if kadane else None
+    clp = (C.c_int * 3)(*clip) if clip else None
+    z = np.ascontiguousarray(np.array(zap, np.float64).reshape(-1), np.float64)
+    L.ref_replot(data.ctypes.data, nchan, nbin, C.c_double(tbin), freqs.ctypes.data, C.c_double(dm),
+                 C.c_double(width), int(zdot), kad, clp, C.c_float(zapthre),
+                 z.ctypes.data if z.size else None, z.size // 2, fd, C.c_float(snrloss), nwidth,
+                 int(pow2bin), int(nopt), upto, out.ctypes.data, out.size, C.byref(nb), C.byref(nc),
+                 C.byref(snr), C.byref(wid), C.byref(dmx), C.byref(mjd), smap.ctypes.data, smap.size,
+                 C.byref(nd))
+    res = {"data": out[:nc.value * nb.value].reshape(nc.value, nb.value), "nbin": nb.value,
+           "nchan": nc.value}
+    if upto >= 12:
+        res.update(snr=np.float32(snr.value), width=np.float32(wid.value), dm_maxsnr=dmx.value,
+                   mjd=mjd.value, ndm=nd.value, snrmap=smap[:nd.value * nb.value].reshape(nd.value, nb.value))
+    return res
 
 
 def ref_boxcar_run(tim, vwn, iqr=False, variant="scalar", nthreads=4):
