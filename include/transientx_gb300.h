@@ -237,6 +237,56 @@ int txg_cluster(const txg_cand *cands, int64_t n, double dms, double ddm, double
 int txg_kadaneF_noalloc(float *x, int64_t ldx, int32_t nchans, int64_t nsamples, int32_t td,
                         int32_t fd, float thr2, int64_t wnlimit, int32_t *ranges, void *stream);
 
+/* ---- replot: the per-candidate chain of replot_fil (replot_fil.cpp:409-457) -------------- */
+/* Options of replot_fil that the chain reads (replot_fil.cpp:49-88 defaults in brackets). */
+typedef struct {
+    int32_t zdot;          /* --zdot: zero-DM matched filter first [0] */
+    int32_t kadane[3];     /* --kadane td fd threshold; kadane[0] = 0 disables [off] */
+    int32_t clip[3];       /* --clip td fd threshold; clip[0] = 0 disables [off] */
+    float zapthre;         /* --zapthre: skewness/kurtosis/autocorrelation IQR cut [3] */
+    int32_t nzap;
+    double zap[16][2];     /* --zap fl fh: channels with fl <= f <= fh set to 0 */
+    int32_t fd;            /* --fd: channel downsample before the search [1] */
+    float snrloss;         /* --snrloss: boxcar width ladder [0.1] */
+    int32_t nwidth;        /* --nw: the data are cut to 2*nw*width [20] */
+    int32_t pow2bin;       /* --pow2bin */
+    int32_t nopt;          /* --nopt: peak search at the candidate DM instead of the DM-time map */
+    int32_t upto;          /* stop after step 1..12 of the chain (0 = all; for checks) */
+} txg_replot_opts;
+
+/* One candidate: its filterbank cut as Candidate::data holds it (one polarisation, channel-major
+ * [nchan][nbin], host memory), sampling time, channel frequencies, the DM and the width (s) of
+ * its .cands line. */
+typedef struct {
+    const float *data;
+    int32_t nchan;
+    int64_t nbin;
+    double tbin;
+    const double *frequencies;
+    double dm;
+    float width;
+} txg_replot_cand;
+
+typedef struct {
+    float snr;             /* Candidate::snr after matched_filter / peak_search */
+    float width;           /* Candidate::width (s) */
+    double dm_maxsnr;      /* Candidate::dm_maxsnr */
+    int64_t maxtid;        /* peak sample: mjd = mjd_start + maxtid*tbin/86400 */
+    int64_t nbin;          /* samples after shrink_to_fit */
+    int32_t nchan;         /* channels after the fd downsample */
+    int32_t ndm;           /* rows of the S/N map (the DM-time map; 1 with nopt) */
+    double dms, ddm;       /* DM axis of the map */
+} txg_replot_result;
+
+/* Runs the chain on n candidates at once on the GPU: [zdot] get_stats, dedisperse (incoherent),
+ * shrink_to_fit(2*nw), azap, zap, get_stats, normalize, [clip], [kadaneF], downsample(1, fd),
+ * then optimize (DM-time Hough transform, hough_transform.h) + matched_filter, or
+ * peak_search (candidate.cpp:56-1200).  snrmap (optional) receives each candidate's S/N map
+ * [ndm][nbin] one after the other; data_out (optional) the data after the last step run. */
+int txg_replot(const txg_replot_opts *opts, const txg_replot_cand *cands, int64_t n,
+               txg_replot_result *out, float *snrmap, int64_t snrmap_cap, float *data_out,
+               int64_t data_cap);
+
 /* Device time per kernel class accumulated since the last call (plan flag TXG_FLAG_TIMING),
  * measured with CUDA events on the handle's stream: ms[c] total milliseconds and launches[c]
  * number of launches of class c; classes 0 unpack, 1 preprocess+RFI, 2 stage 1,

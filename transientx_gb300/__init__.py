@@ -52,6 +52,25 @@ class txg_row(C.Structure):
     ]
 
 
+class txg_replot_opts(C.Structure):
+    _fields_ = [("zdot", C.c_int32), ("kadane", C.c_int32 * 3), ("clip", C.c_int32 * 3),
+                ("zapthre", C.c_float), ("nzap", C.c_int32), ("zap", (C.c_double * 2) * 16),
+                ("fd", C.c_int32), ("snrloss", C.c_float), ("nwidth", C.c_int32),
+                ("pow2bin", C.c_int32), ("nopt", C.c_int32), ("upto", C.c_int32)]
+
+
+class txg_replot_cand(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("nchan", C.c_int32), ("nbin", C.c_int64),
+                ("tbin", C.c_double), ("frequencies", C.c_void_p), ("dm", C.c_double),
+                ("width", C.c_float)]
+
+
+class txg_replot_result(C.Structure):
+    _fields_ = [("snr", C.c_float), ("width", C.c_float), ("dm_maxsnr", C.c_double),
+                ("maxtid", C.c_int64), ("nbin", C.c_int64), ("nchan", C.c_int32),
+                ("ndm", C.c_int32), ("dms", C.c_double), ("ddm", C.c_double)]
+
+
 class txg_result(C.Structure):
     _fields_ = [("counter", C.c_int64), ("gated", C.c_int32), ("overflow", C.c_int32),
                 ("npoints", C.c_int64), ("nclusters", C.c_int64)]
@@ -86,7 +105,7 @@ EXPORTS = [
     "txg_get_block", "txg_get_zap_ranges", "txg_get_tables", "txg_width_ladder", "txg_boxcar",
     "txg_cluster", "txg_get_timing", "txg_get_stream", "txg_strerror", "txg_version",
     "txg_describe_row", "txg_pop_result", "txg_get_mask", "txg_kadaneF_noalloc",
-    "txg_get_subdata", "txg_cand_band",
+    "txg_get_subdata", "txg_cand_band", "txg_replot",
 ]
 
 _lib: Optional[C.CDLL] = None
@@ -129,6 +148,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.txg_get_stream.argtypes = [vp, C.POINTER(vp)]
     L.txg_get_mask.argtypes = [vp, C.c_int32, vp]
     L.txg_get_subdata.argtypes = [vp, C.c_int32, C.c_int32, C.c_int64, vp]
+    L.txg_replot.argtypes = [C.POINTER(txg_replot_opts), C.POINTER(txg_replot_cand), C.c_int64,
+                             C.POINTER(txg_replot_result), vp, C.c_int64, vp, C.c_int64]
     L.txg_cand_band.argtypes = [vp, C.c_int32, C.c_int32, vp, C.c_int64, vp, vp]
     L.txg_kadaneF_noalloc.argtypes = [vp, C.c_int64, C.c_int32, C.c_int64, C.c_int32, C.c_int32,
                                       C.c_float, C.c_int64, vp, vp]
@@ -508,3 +529,54 @@ def cluster(cands: np.ndarray, dms: float, ddm: float, fmax: float, fmin: float,
                                       int(drop), maxwn, _ptr(out), len(out), C.byref(n)),
            "txg_cluster")
     return out[: n.value].copy()
+
+
+def replot(cands, zdot: bool = False, kadane=None, clip=None, zapthre: float = 3.0, zap=(),
+           fd: int = 1, snrloss: float = 0.1, nwidth: int = 20, pow2bin: bool = False,
+           nopt: bool = False, upto: int = 0, maps: bool = False, data: bool = False):
+    """The replot_fil chain (replot_fil.cpp:409-457) on the GPU for a batch of candidates, each a
+    dict with data [nchan][nbin] float32, tbin, frequencies, dm, width (s).  Returns a list of
+    dicts (snr, width, dm_maxsnr, maxtid, nbin, nchan, ndm, dms, ddm), with the S/N map and/or
+    the final data when asked."""
+    L = load_library()
+    o = txg_replot_opts()
+    o.zdot = int(zdot)
+    for i, v in enumerate(kadane or (0, 0, 0)):
+        o.kadane[i] = int(v)
+    for i, v in enumerate(clip or (0, 0, 0)):
+        o.clip[i] = int(v)
+    o.zapthre = zapthre
+    o.nzap = len(zap)
+    for i, (a, b) in enumerate(zap):
+        o.zap[i][0], o.zap[i][1] = a, b
+    o.fd, o.snrloss, o.nwidth, o.pow2bin, o.nopt, o.upto = fd, snrloss, nwidth, int(pow2bin), int(nopt), upto
+    keep = []
+    arr = (txg_replot_cand * len(cands))()
+    for k, c in enumerate(cands):
+        d = np.ascontiguousarray(c["data"], np.float32)
+        f = np.ascontiguousarray(c["frequencies"], np.float64)
+        keep += [d, f]
+        arr[k].data, arr[k].nchan, arr[k].nbin = d.ctypes.data, d.shape[0], d.shape[1]
+        arr[k].tbin, arr[k].frequencies = c["tbin"], f.ctypes.data
+        arr[k].dm, arr[k].width = c["dm"], c["width"]
+    res = (txg_replot_result * len(cands))()
+    total = sum(np.asarray(c["data"]).size for c in cands)
+    mapcap = sum(int(2 ** np.ceil(np.log2(max(2, np.asarray(c["data"]).shape[0])))) *
+                 np.asarray(c["data"]).shape[1] for c in cands)
+    smap = np.zeros(mapcap if maps else 0, np.float32)
+    dout = np.zeros(total if data else 0, np.float32)
+    _check(L.txg_replot(C.byref(o), arr, len(cands), res, _ptr(smap) if maps else None, smap.size,
+                        _ptr(dout) if data else None, dout.size), "replot")
+    out, pm, pd = [], 0, 0
+    for r in res:
+        d = {k: getattr(r, k) for k, _ in txg_replot_result._fields_}
+        if maps and d["ndm"] > 0:
+            cnt = d["ndm"] * d["nbin"]
+            d["snrmap"] = smap[pm:pm + cnt].reshape(d["ndm"], d["nbin"])
+            pm += cnt
+        if data:
+            cnt = d["nchan"] * d["nbin"]
+            d["data"] = dout[pd:pd + cnt].reshape(d["nchan"], d["nbin"])
+            pd += cnt
+        out.append(d)
+    return out

@@ -14,7 +14,11 @@ LIB = os.path.join(PKG, "libtxgpu.so")
 SYNTH = os.path.join(PKG, "libtxsynth.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SRC = ["txg_pre.cu", "txg_dedisp.cu", "txg_boxcar.cu", "txg_api.cu", "txg_noalloc.cu"]
+CU_SRC = ["txg_pre.cu", "txg_dedisp.cu", "txg_boxcar.cu", "txg_api.cu", "txg_noalloc.cu",
+          "txg_replot.cu"]
+# files whose device arithmetic follows the reference's mixed float/double expressions as
+# written: no multiply-add contraction anywhere in them
+NO_FMAD = {"txg_replot.cu"}
 CPP_SRC = ["txg_plan.cpp", "txg_cluster.cpp"]
 
 
@@ -55,6 +59,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
         if force or _stale(o, [s] + headers):
             cmd = [nv, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
                    "-c", s, "-o", o]
+            if src in NO_FMAD:
+                cmd.insert(1, "-fmad=false")
             if verbose:
                 cmd.insert(1, "-Xptxas=-v")
             jobs.append(cmd)
