@@ -42,6 +42,8 @@ def parse_args():
     ap.add_argument("--workload", default="nchan4096_n2M_rfi_dm3000")
     ap.add_argument("--nsamples", type=int, default=0, help="override the file length")
     ap.add_argument("--precision", choices=["fp32", "bf16", "fp16"], default="fp32")
+    ap.add_argument("--replot", type=int, default=0,
+                    help="time the replot chain on this many 4096-channel candidates instead")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-blocks", type=int, default=2, help="timed oracle blocks (CPU baseline)")
@@ -372,8 +374,36 @@ def run_ours(args, wl):
     print(json.dumps(line), flush=True)
 
 
+def run_replot(args):
+    """Replot chain throughput: one batch of candidates through transientx_gb300.replot (host
+    buffers in, results out) per step, wall time."""
+    import transientx_gb300 as tx
+    from transientx_gb300 import synth
+    cands = synth.replot_candidates(args.replot)
+    for _ in range(args.warmup):
+        tx.replot(cands)
+    ts = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        r = tx.replot(cands)
+        ts.append(time.perf_counter() - t)
+    per = float(np.median(ts))
+    line = {"metric": "replot candidates/s", "value": args.replot / per, "unit": "candidates/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3,
+            "higher_is_better": True, "data": "synthetic",
+            "config": {"workload": "replot_nchan4096", "candidates": args.replot,
+                       "shape": list(cands[0]["data"].shape), "tbin": cands[0]["tbin"],
+                       "dm": cands[0]["dm"], "width": cands[0]["width"]},
+            "ms_per_candidate": per * 1e3 / args.replot,
+            "first": {"snr": r[0]["snr"], "dm_maxsnr": r[0]["dm_maxsnr"], "maxtid": r[0]["maxtid"]}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
+    if args.replot:
+        run_replot(args)
+        return
     from transientx_gb300 import synth
     make = synth.WORKLOADS[args.workload]
     wl = make(nsamples=args.nsamples) if args.nsamples else make()

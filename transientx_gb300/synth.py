@@ -177,5 +177,27 @@ def nchan8192_dm5000(seed: int = 5, nsamples: int = 1 << 23) -> Workload:
     return Workload("nchan8192_n8M_dm5000", fil, rows, seglen_ndump(tsamp, [1, 2, 4, 8, 16]))
 
 
+def replot_candidates(n: int, nchan: int = 4096, seed: int = 9, dm: float = 500.0,
+                      width: float = 2e-3, tbin: float = 76e-6, nwidth: int = 20):
+    """Candidates as replot_fil cuts them (replot_fil.cpp:300-306): nbin = (delay across the
+    band + 2*nw*width)/tbin samples of integer-valued noise of 4096 channels 1712-856 MHz with
+    a dispersed pulse, one dict per candidate for transientx_gb300.replot."""
+    f = band(nchan, 1712.0, 856.0)
+    k = 4.148741601e3
+    dly = k * dm * (1.0 / f.min() ** 2 - 1.0 / f.max() ** 2)
+    nbin = int((dly + 2 * nwidth * width) / tbin)
+    wb = max(1, int(width / tbin))
+    out = []
+    for c in range(n):
+        rng = np.random.default_rng(seed + c)
+        x = np.round(rng.normal(100.0, 10.0, (nchan, nbin))).astype(np.float32)
+        t0 = 0.4 * nbin * tbin
+        for j in range(nchan):
+            i0 = int((t0 + k * dm * (1.0 / f[j] ** 2 - 1.0 / f.max() ** 2)) / tbin) % nbin
+            x[j, i0:i0 + wb] += 3.0
+        out.append({"data": x, "frequencies": f, "tbin": tbin, "dm": dm, "width": width})
+    return out
+
+
 WORKLOADS = {"nchan256_n1M_dm1000": nchan256_single, "nchan4096_n2M_rfi_dm3000": nchan4096_rfi,
              "nchan8192_n8M_dm5000": nchan8192_dm5000}
