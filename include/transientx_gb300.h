@@ -169,6 +169,16 @@ int txg_get_dense(txg_handle *h, int32_t beam, int32_t row, float *mxS, int32_t 
 int txg_get_timdata(txg_handle *h, int32_t beam, int32_t row, int64_t idm0, int64_t count,
                     float *out);
 
+/* The dedispersed series of DMs idm0..idm0+count-1 of the last block quantised for dumping
+ * (the --savetim/--mean/--std/--nbits output of SubbandDedispersion::rundump,
+ * singlepulse.cpp:237-238,339-340, dedisperse_fil.cpp:95-99): each series standardised by its
+ * own mean and standard deviation over its first nsamp samples, then z*std + mean as float
+ * (nbits 32) or rounded to even and clamped to 0..255 / 0..65535 (nbits 8 / 16).  out:
+ * [count][nsamp] of that type.  Pass nsamp = ndump to dump consecutive blocks without the
+ * overlap. */
+int txg_get_timdata_q(txg_handle *h, int32_t beam, int32_t row, int64_t idm0, int64_t count,
+                      int64_t nsamp, int32_t nbits, float mean, float std, void *out);
+
 /* The row's preprocessed block after the rfilist ([nchans][ndump], TXG_FLAG_KEEP_SERIES),
  * and the zapped windows of rfilist entry irfi: kadaneF [nchans/fd][4] (start,end of the
  * positive and negative window in block samples, -1 if not zapped); kadaneT [ndump/td][4]

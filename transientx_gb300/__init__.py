@@ -105,7 +105,7 @@ EXPORTS = [
     "txg_get_block", "txg_get_zap_ranges", "txg_get_tables", "txg_width_ladder", "txg_boxcar",
     "txg_cluster", "txg_get_timing", "txg_get_stream", "txg_strerror", "txg_version",
     "txg_describe_row", "txg_pop_result", "txg_get_mask", "txg_kadaneF_noalloc",
-    "txg_get_subdata", "txg_cand_band", "txg_replot",
+    "txg_get_subdata", "txg_cand_band", "txg_replot", "txg_get_timdata_q",
 ]
 
 _lib: Optional[C.CDLL] = None
@@ -148,6 +148,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.txg_get_stream.argtypes = [vp, C.POINTER(vp)]
     L.txg_get_mask.argtypes = [vp, C.c_int32, vp]
     L.txg_get_subdata.argtypes = [vp, C.c_int32, C.c_int32, C.c_int64, vp]
+    L.txg_get_timdata_q.argtypes = [vp, C.c_int32, C.c_int32, C.c_int64, C.c_int64, C.c_int64,
+                                    C.c_int32, C.c_float, C.c_float, vp]
     L.txg_replot.argtypes = [C.POINTER(txg_replot_opts), C.POINTER(txg_replot_cand), C.c_int64,
                              C.POINTER(txg_replot_result), vp, C.c_int64, vp, C.c_int64]
     L.txg_cand_band.argtypes = [vp, C.c_int32, C.c_int32, vp, C.c_int64, vp, vp]
@@ -423,6 +425,19 @@ class Search:
         out = np.zeros((count, i.nsamples), np.float32)
         _check(load_library().txg_get_timdata(self.h, beam, row, idm0, count, _ptr(out)),
                "timdata")
+        return out
+
+    def timdata_q(self, row: int = 0, beam: int = 0, idm0: int = 0, count: int = -1,
+                  nsamp: int = 0, nbits: int = 8, mean: float = 0.0, std: float = 3.0) -> np.ndarray:
+        """Quantised dedispersed series of the last block ([count][nsamp] uint8 / uint16 /
+        float32; nsamp 0 = ndump, the non-overlapping part)."""
+        i = self.row_info(row, beam)
+        count = i.ndm - idm0 if count < 0 else count
+        nsamp = i.ndump if nsamp <= 0 else nsamp
+        dt = {8: np.uint8, 16: np.uint16, 32: np.float32}[nbits]
+        out = np.zeros((count, nsamp), dt)
+        _check(load_library().txg_get_timdata_q(self.h, beam, row, idm0, count, nsamp, nbits, mean,
+                                                std, _ptr(out)), "timdata_q")
         return out
 
     def subdata(self, idm: int, row: int = 0, beam: int = 0) -> np.ndarray:

@@ -946,6 +946,77 @@ int txg_get_timdata(txg_handle *h, int32_t beam, int32_t row, int64_t idm0, int6
     return TXG_OK;
 }
 
+/* Dedispersed series of DMs [idm0, idm0+count) of the last block, each standardised by its own
+ * mean and standard deviation over the first nsamp samples (double, lane-strided), then
+ * scaled to out = z*ostd + omean: nbits 32 -> float, 16/8 -> round-to-even, clamped to the
+ * unsigned range. */
+__global__ void k_tim_quant(const float *__restrict__ tim, long ldt, long nsamp, int nbits,
+                            float omean, float ostd, void *__restrict__ out)
+{
+    const long k = blockIdx.x;
+    const float *r = tim + k * ldt;
+    __shared__ double red[2][32];
+    double s1 = 0., s2 = 0.;
+    for (long i = threadIdx.x; i < nsamp; i += blockDim.x) {
+        const double v = r[i];
+        s1 = __dadd_rn(s1, v);
+        s2 = __dadd_rn(s2, __dmul_rn(v, v));
+    }
+    for (int off = 16; off >= 1; off >>= 1) {
+        s1 = __dadd_rn(s1, __shfl_xor_sync(0xffffffffu, s1, off));
+        s2 = __dadd_rn(s2, __shfl_xor_sync(0xffffffffu, s2, off));
+    }
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    if (lane == 0) {
+        red[0][w] = s1;
+        red[1][w] = s2;
+    }
+    __syncthreads();
+    double a = 0., b = 0.;
+    for (int q = 0; q < nw; q++) {
+        a = __dadd_rn(a, red[0][q]);
+        b = __dadd_rn(b, red[1][q]);
+    }
+    const double mean = __ddiv_rn(a, (double)nsamp);
+    const double var = __dsub_rn(__ddiv_rn(b, (double)nsamp), __dmul_rn(mean, mean));
+    const double sd = var > 0. ? __dsqrt_rn(var) : 1.;
+    for (long i = threadIdx.x; i < nsamp; i += blockDim.x) {
+        const double z = __ddiv_rn(__dsub_rn((double)r[i], mean), sd);
+        const float q = __double2float_rn(__dadd_rn(__dmul_rn(z, (double)ostd), (double)omean));
+        if (nbits == 32) {
+            reinterpret_cast<float *>(out)[k * nsamp + i] = q;
+        } else {
+            const float hi = nbits == 16 ? 65535.f : 255.f;
+            const float c = fminf(fmaxf(rintf(q), 0.f), hi);
+            if (nbits == 16) reinterpret_cast<uint16_t *>(out)[k * nsamp + i] = (uint16_t)c;
+            else reinterpret_cast<uint8_t *>(out)[k * nsamp + i] = (uint8_t)c;
+        }
+    }
+}
+
+int txg_get_timdata_q(txg_handle *h, int32_t beam, int32_t row, int64_t idm0, int64_t count,
+                      int64_t nsamp, int32_t nbits, float mean, float std, void *out)
+{
+    int rc = check_beam_row(h, beam, row);
+    if (rc) return rc;
+    const RowPlan &P = h->rp[row];
+    if (!out || idm0 < 0 || count < 1 || idm0 + count > P.cfg.ndm) return fail(TXG_ERR_ARG, "DM range");
+    if (nsamp < 1 || nsamp > P.nout) return fail(TXG_ERR_ARG, "nsamp must be 1..nsamples");
+    if (nbits != 8 && nbits != 16 && nbits != 32) return fail(TXG_ERR_ARG, "nbits must be 8, 16 or 32");
+    const size_t bytes = (size_t)count * nsamp * (nbits / 8);
+    void *d = nullptr;
+    TXG_CUDA_TRY(cudaStreamSynchronize(h->st));
+    TXG_CUDA_TRY(cudaMalloc(&d, bytes));
+    k_tim_quant<<<(unsigned)count, 256, 0, h->st>>>(h->br[beam][row].tim + idm0 * P.nout, P.nout, nsamp,
+                                                    nbits, mean, std, d);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    if (e == cudaSuccess) e = cudaMemcpy(out, d, bytes, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return set_cuda_error(e, "txg_get_timdata_q", __FILE__, __LINE__);
+    return TXG_OK;
+}
+
 int txg_get_block(txg_handle *h, int32_t beam, int32_t row, float *out)
 {
     int rc = check_beam_row(h, beam, row);
