@@ -119,17 +119,23 @@ def class_bytes(info, sp, nchans_raw, ndump_raw, ncand, elem):
             series + 4.0 * info.ndm * info.nsamples, 4.0 * info.ndm * info.nsamples + 16 * ncand]
 
 
-def launches_per_block(sp, info, gated):
-    n = 2  # unpack, equalize
-    if info.nchans and sp.bswidth > 0:
-        n += 3
+RFI_LAUNCHES = {"kadaneF": 3, "kadaneT": 3, "zdot": 4, "zero": 2, "mask": 10}
+BOXCAR_ROW_MAX = 51200  # samples of a dedispersed row one boxcar CTA holds; longer rows: 2 kernels
+
+
+def launches_per_block(sp, info, gated, precision="fp32"):
+    """Kernels one block launches for one ddplan row (txg_api.cu run_block)."""
+    n = 2  # unpack, equalize parameters
+    n += 3 if sp.bswidth > 0 else 1  # colmean, smooth, equalize+baseline apply | apply
     if sp.zaplist:
         n += 1
     for op in sp.rfilist:
-        n += 3 if op[0] == "kadaneF" else 4
+        n += RFI_LAUNCHES[op[0]]
+    if precision != "fp32":
+        n += 1  # FP16 copy of the block
     n += 1  # stage 1
     if gated:
-        n += 2  # stage 2, boxcar
+        n += 1 + (2 if info.nsamples > BOXCAR_ROW_MAX else 1)  # stage 2, boxcar
     return n
 
 
@@ -242,9 +248,9 @@ def run_ours(args, wl):
                     stats["work"] += infos[r].ndm * infos[r].nsamples
                     stats["ncand"][r] += res.npoints
                     stats["gated"][r] += 1
-                    stats["launches"] += launches_per_block(wl.rows[r], infos[r], True)
+                    stats["launches"] += launches_per_block(wl.rows[r], infos[r], True, args.precision)
                 else:
-                    stats["launches"] += launches_per_block(wl.rows[r], infos[r], False)
+                    stats["launches"] += launches_per_block(wl.rows[r], infos[r], False, args.precision)
 
     def new_stats():
         return {"work": 0, "ncand": [0] * len(wl.rows), "gated": [0] * len(wl.rows),

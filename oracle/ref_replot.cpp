@@ -13,6 +13,11 @@
 
 #include "candidate.h"
 
+/* the reference's thread-count global (defined in ref_harness.cpp).  Candidate::peak_search
+ * adds channels into the shared profile inside an OpenMP loop over channels
+ * (candidate.cpp:1113-1121), a data race with more than one thread: the chain runs with one. */
+extern unsigned int num_threads;
+
 extern "C" int ref_replot(const float *data, int nchan, long nbin, double tbin, const double *freqs,
                           double dm, double width, int zdot, const int *kadane, const int *clip,
                           float zapthre, const double *zap, int nzap, int fd, float snrloss,
@@ -21,6 +26,7 @@ extern "C" int ref_replot(const float *data, int nchan, long nbin, double tbin, 
                           double *dm_maxsnr, double *mjd, float *snrmap, long snrmap_cap,
                           int *ndm_out)
 {
+    num_threads = 1;
     Candidate c;
     c.npol = 1;
     c.nchan = nchan;

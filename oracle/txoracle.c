@@ -238,13 +238,15 @@ void txo_equalize(float *x, int nchan, long n, long ldx, uint8_t *live)
     }
 }
 
-/* Channel sum at sample i in the fixed order both implementations use: 8 consecutive
- * channel blocks of ceil(nchan/8), each summed from 0.0f, block sums added in order. */
-static float colsum8(const float *x, int nchan, long ldx, long i)
+/* Channel sum at sample i in the fixed order both implementations use: 32 consecutive
+ * channel blocks of ceil(nchan/32), each summed from 0.0f, block sums (empty blocks
+ * included) added in order. */
+#define COLSUM_BLK 32
+static float colsum(const float *x, int nchan, long ldx, long i)
 {
-    const int cb = (nchan + 7) / 8;
+    const int cb = (nchan + COLSUM_BLK - 1) / COLSUM_BLK;
     float t = 0.f;
-    for (int q = 0; q < 8; q++) {
+    for (int q = 0; q < COLSUM_BLK; q++) {
         float acc = 0.f;
         const int j1 = (q + 1) * cb < nchan ? (q + 1) * cb : nchan;
         for (int j = q * cb; j < j1; j++) acc = acc + x[(long)j * ldx + i];
@@ -271,7 +273,7 @@ void txo_baseline(float *x, int nchan, long n, long ldx, long nw, const uint8_t 
         return;
     }
 #pragma omp parallel for num_threads(nthr())
-    for (long i = 0; i < n; i++) z[i] = colsum8(x, nchan, ldx, i) / (float)nlive;
+    for (long i = 0; i < n; i++) z[i] = colsum(x, nchan, ldx, i) / (float)nlive;
 #pragma omp parallel for num_threads(nthr())
     for (long i = 0; i < n; i++) {
         long lo = i - h < 0 ? 0 : i - h;
@@ -501,7 +503,7 @@ void txo_zdot(float *x, int nchan, long n, long ldx)
         for (long i = 0; i < n; i++) r[i] = (r[i] - mf) * inv;
     }
 #pragma omp parallel for num_threads(nthr())
-    for (long i = 0; i < n; i++) s[i] = colsum8(x, nchan, ldx, i) / (float)nchan;
+    for (long i = 0; i < n; i++) s[i] = colsum(x, nchan, ldx, i) / (float)nchan;
     double se = txo_red32(s, 0, n, 0), ss = txo_red32(s, 0, n, 1);
     double tmp = se * se - ss * (double)n;
 #pragma omp parallel for num_threads(nthr())

@@ -176,6 +176,8 @@ struct BeamRow {
     float *z = nullptr, *b = nullptr, *s = nullptr;
     double *sst = nullptr;
     uint8_t *live = nullptr;
+    unsigned long long *eqpart = nullptr; /* equalize: per-(channel, 64-sample tile) sums */
+    float2 *eqp = nullptr, *zp = nullptr; /* (mean, 1/sd) per channel: equalize, zdot */
     void *ring = nullptr;
     float *tim = nullptr;
     double *bx_scratch = nullptr; /* boxcar statistics and chunk offsets of long rows */
@@ -475,14 +477,18 @@ int run_block(txg_handle *h, int beam, const uint8_t *raw)
                                            P.ldh * sizeof(float), P.H * sizeof(float), P.C,
                                            cudaMemcpyDeviceToDevice, h->st));
         float *x = xcur + P.H;
-        launch_unpack(raw, Craw, n0, P.cfg.td, P.cfg.fd, x, P.ldh, P.C, P.N, mask, h->st);
+        const bool part = launch_unpack(raw, Craw, n0, P.cfg.td, P.cfg.fd, x, P.ldh, P.C, P.N, mask,
+                                        b.eqpart, h->st);
         if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[1], h->st));
 
-        launch_equalize(x, P.ldh, P.C, P.N, b.live, h->st);
+        /* equalize from the unpack's integer sums; its apply rides on the baseline pass */
+        launch_eq_params(part ? b.eqpart : nullptr, x, P.ldh, P.C, P.N, b.eqp, b.live, h->st);
         if (P.bl_nw > 0) {
-            launch_colmean(x, P.ldh, P.C, P.N, b.live, b.z, h->st);
+            launch_colmean(x, P.ldh, P.C, P.N, b.live, b.eqp, b.z, h->st);
             launch_smooth(b.z, P.N, P.bl_nw, b.b, h->st);
-            launch_sub_series(x, P.ldh, P.C, P.N, b.b, b.live, h->st);
+            launch_eq_apply(x, P.ldh, P.C, P.N, b.eqp, b.b, b.live, h->st);
+        } else {
+            launch_eq_apply(x, P.ldh, P.C, P.N, b.eqp, nullptr, b.live, h->st);
         }
         if (!P.zap_chan.empty())
             launch_zero_rows(x, P.ldh, D.zap, (int)P.zap_chan.size(), P.N, h->st);
@@ -491,7 +497,7 @@ int run_block(txg_handle *h, int beam, const uint8_t *raw)
                 launch_kadane(x, P.ldh, P.C, P.N, P.cfg.rfi_td[q], P.cfg.rfi_fd[q], P.kad_thr,
                               P.kad_wnlimit[q], b.ds, b.ranges[q], h->st);
             else if (P.cfg.rfi_kind[q] == TXG_RFI_ZDOT)
-                launch_zdot(x, P.ldh, P.C, P.N, b.s, b.sst, h->st);
+                launch_zdot(x, P.ldh, P.C, P.N, b.s, b.sst, b.zp, h->st);
             else if (P.cfg.rfi_kind[q] == TXG_RFI_KADANET)
                 launch_kadaneT(x, P.ldh, P.C, P.N, P.cfg.rfi_td[q], P.cfg.rfi_fd[q], P.kadT_thr,
                                P.kad_wnlimit[q], b.ds, b.ranges[q], h->st);
@@ -500,7 +506,7 @@ int run_block(txg_handle *h, int beam, const uint8_t *raw)
                             b.sel, b.ranges[q], h->st);
             else if (P.cfg.rfi_kind[q] == TXG_RFI_ZERO) {
                 /* zero-DM filter: the live-channel mean series off every live channel */
-                launch_colmean(x, P.ldh, P.C, P.N, b.live, b.z, h->st);
+                launch_colmean(x, P.ldh, P.C, P.N, b.live, nullptr, b.z, h->st);
                 launch_sub_series(x, P.ldh, P.C, P.N, b.z, b.live, h->st);
             }
         }
@@ -763,7 +769,9 @@ int txg_create(const txg_plan *plan, txg_handle **out)
             if ((rc = dalloc(h, &b.ds, (size_t)kmax)) || (rc = dalloc(h, &b.z, (size_t)P.N)) ||
                 (rc = dalloc(h, &b.live, (size_t)P.C)) ||
                 (rc = dalloc(h, &b.b, (size_t)P.N)) || (rc = dalloc(h, &b.s, (size_t)P.N)) ||
-                (rc = dalloc(h, &b.sst, (size_t)2)))
+                (rc = dalloc(h, &b.sst, (size_t)2)) ||
+                (rc = dalloc(h, &b.eqpart, (size_t)2 * P.C * eq_part_tiles(P.N))) ||
+                (rc = dalloc(h, &b.eqp, (size_t)P.C)) || (rc = dalloc(h, &b.zp, (size_t)P.C)))
                 return bail(rc);
             unsigned char *ring = nullptr;
             if ((rc = dalloc(h, &ring, (size_t)P.ng * P.nsub * P.R * ring_elem(h->prec)))) return bail(rc);

@@ -74,6 +74,14 @@ __device__ __forceinline__ void fence_proxy_async()
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
+/* 4-byte asynchronous global->shared copies (completion per thread by group). */
+__device__ __forceinline__ void cp_async4(void *dst, const void *src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
 /* Bounded wait on phase `parity`; returns false if it gave up. */
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
 {
@@ -210,19 +218,34 @@ k_stage1r(const float *__restrict__ xh, long ldh, long col0, int C, long N, int 
     __shared__ __align__(8) uint64_t bar;
     __shared__ int span_sh;
     float *win = reinterpret_cast<float *>(smraw);
-    int32_t *dsm = reinterpret_cast<int32_t *>(win + (size_t)maxch * wmax);
+    int32_t *dsm = reinterpret_cast<int32_t *>(win + (size_t)maxch * wmax); /* 2 x [maxch][GPC] */
     const int s = blockIdx.y;
     const long u0 = (long)blockIdx.x * TT;
     const int j0 = sub_start[s], j1 = sub_start[s + 1], jn = j1 - j0;
     const int tid = threadIdx.x, lt = tid % TH, gs = tid / TH;
     const long cstart = (u0 + col0) & ~3L;
     const int al = (int)(u0 + col0 - cstart);
+    const int nch = (ng + GPC - 1) / GPC;
+    /* delays of chunk c (groups past the end repeat the last one) into table buffer c & 1 */
+    auto fetch = [&](int c) {
+        if (c < nch) {
+            const int g0 = c * GPC, gn = min(GPC, ng - g0);
+            int32_t *dt = dsm + (size_t)(c & 1) * maxch * GPC;
+#pragma unroll 1
+            for (int e = tid; e < jn * GPC; e += NT) {
+                const int jj = e / GPC, g = e % GPC;
+                cp_async4(&dt[e], &d1[(size_t)(g0 + (g < gn ? g : gn - 1)) * C + j0 + jj]);
+            }
+        }
+        cp_async_commit();
+    };
 
     if (tid == 0) {
         mbar_init(&bar, 1);
         fence_mbar_init();
         span_sh = 0;
     }
+    fetch(0);
     __syncthreads();
     for (int jj = tid; jj < jn; jj += NT) atomicMax(&span_sh, d1[(size_t)(ng - 1) * C + j0 + jj]);
     __syncthreads();
@@ -237,16 +260,15 @@ k_stage1r(const float *__restrict__ xh, long ldh, long col0, int C, long N, int 
     if (!__syncthreads_and(ok)) {
         if (tid == 0) atomicExch(err, 1);
         mbar_wait(&bar, 0);
+        cp_async_wait_all();
         return;
     }
-    for (int g0 = 0; g0 < ng; g0 += GPC) {
-        const int gn = min(GPC, ng - g0);
-        /* delays of the chunk; groups past the end repeat the last one (no reload) */
-        for (int e = tid; e < jn * GPC; e += NT) {
-            const int jj = e / GPC, g = e % GPC;
-            dsm[e] = d1[(size_t)(g0 + (g < gn ? g : gn - 1)) * C + j0 + jj];
-        }
-        __syncthreads();
+    for (int c = 0; c < nch; c++) {
+        const int g0 = c * GPC, gn = min(GPC, ng - g0);
+        cp_async_wait_all(); /* this thread's copies of chunk c */
+        __syncthreads();     /* everyone's; and buffer (c+1)&1 is no longer read */
+        fetch(c + 1);        /* overlaps this chunk's sums */
+        const int32_t *dtab = dsm + (size_t)(c & 1) * maxch * GPC;
         float acc[GPT][U];
 #pragma unroll
         for (int g = 0; g < GPT; g++)
@@ -254,7 +276,7 @@ k_stage1r(const float *__restrict__ xh, long ldh, long col0, int C, long N, int 
             for (int q = 0; q < U; q++) acc[g][q] = 0.f;
         for (int jj = 0; jj < jn; jj++) {
             const float *wr = win + (size_t)jj * W + al + lt;
-            const int4 *dv = reinterpret_cast<const int4 *>(dsm + jj * GPC + gs * GPT);
+            const int4 *dv = reinterpret_cast<const int4 *>(dtab + jj * GPC + gs * GPT);
             int dd[GPT];
 #pragma unroll
             for (int gq = 0; gq < GPT / 4; gq++) {
@@ -285,7 +307,6 @@ k_stage1r(const float *__restrict__ xh, long ldh, long col0, int C, long N, int 
                 }
             }
         }
-        __syncthreads();
     }
 }
 
@@ -347,7 +368,23 @@ k_stage1p(const __half *__restrict__ xh, long ldh, long col0, int C, long N, int
     const long ES = (W + 8) / 2;                             /* even-pair words per channel */
     const long OS = W / 2;                                   /* odd-pair words per channel */
     uint32_t *ew = words, *ow = words + (size_t)jn * ES;
-    int32_t *dsm = reinterpret_cast<int32_t *>(ow + (size_t)jn * OS);
+    /* after the windows (sized for wmax): raw delays of the next chunk, then the word offsets
+     * of the current one */
+    int32_t *raw = reinterpret_cast<int32_t *>(words + (size_t)maxch * ((wmax + 8) / 2 + wmax / 2));
+    int32_t *dsm = raw + (size_t)maxch * GPC;
+    const int nch = (ng + GPC - 1) / GPC;
+    auto fetch = [&](int c) { /* delays of chunk c (groups past the end repeat the last one) */
+        if (c < nch) {
+            const int g0 = c * GPC, gn = min(GPC, ng - g0);
+#pragma unroll 1
+            for (int e = tid; e < jn * GPC; e += NT) {
+                const int jj = e / GPC, g = e % GPC;
+                cp_async4(&raw[e], &d1[(size_t)(g0 + (g < gn ? g : gn - 1)) * C + j0 + jj]);
+            }
+        }
+        cp_async_commit();
+    };
+    fetch(0);
     if (tid == 0) {
         const uint32_t bytes = (uint32_t)(W * sizeof(__half));
         mbar_expect_tx(&bar, bytes * (uint32_t)jn);
@@ -358,19 +395,23 @@ k_stage1p(const __half *__restrict__ xh, long ldh, long col0, int C, long N, int
     if (!__syncthreads_and(ok)) {
         if (tid == 0) atomicExch(err, 1);
         mbar_wait(&bar, 0);
+        cp_async_wait_all();
         return;
     }
     for (int jj = 0; jj < jn; jj++) build_odd(ew + (size_t)jj * ES, ow + (size_t)jj * OS, OS, tid, NT);
-    for (int g0 = 0; g0 < ng; g0 += GPC) {
-        const int gn = min(GPC, ng - g0);
+    for (int c = 0; c < nch; c++) {
+        cp_async_wait_all(); /* this thread's copies of chunk c */
+        __syncthreads();     /* everyone's; the previous chunk's offsets are no longer read */
         /* word offset of the pair at (channel, delay): even or odd copy by the parity */
         for (int e = tid; e < jn * GPC; e += NT) {
-            const int jj = e / GPC, g = e % GPC;
-            const int h = al + d1[(size_t)(g0 + (g < gn ? g : gn - 1)) * C + j0 + jj];
+            const int jj = e / GPC;
+            const int h = al + raw[e];
             dsm[e] = (h & 1) ? (int)((size_t)jn * ES + (size_t)jj * OS + (h - 1) / 2)
                              : (int)((size_t)jj * ES + h / 2);
         }
         __syncthreads();
+        fetch(c + 1); /* overlaps this chunk's sums */
+        const int g0 = c * GPC, gn = min(GPC, ng - g0);
         float acc[GPT][2 * UP];
 #pragma unroll
         for (int g = 0; g < GPT; g++)
@@ -410,7 +451,6 @@ k_stage1p(const __half *__restrict__ xh, long ldh, long col0, int C, long N, int
                 }
             }
         }
-        __syncthreads();
     }
 }
 
@@ -721,7 +761,7 @@ static bool stage1r_try(const float *xh, long ldh, long col0, int C, long N, int
 {
     const long tt = (long)TH * U;
     const long wr = (tt + maxd1 + 3 + 3) / 4 * 4;
-    const size_t smem = (size_t)maxch * wr * sizeof(float) + (size_t)maxch * GS * GPT * sizeof(int32_t);
+    const size_t smem = (size_t)maxch * wr * sizeof(float) + 2 * (size_t)maxch * GS * GPT * sizeof(int32_t);
     if (smem > RESIDENT_BUDGET) return false;
     auto kern = k_stage1r<T, TH, U, GS, GPT>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -738,7 +778,7 @@ static bool stage1p_try(const __half *x16, long ldh, long col0, int C, long N, i
     const long tt = 2L * TH * UP;
     const long w = (tt + maxd1 + 7 + 2 + 7) / 8 * 8;
     const size_t smem =
-        (size_t)maxch * ((w + 8) * 2 + w * 2) + (size_t)maxch * GS * GPT * sizeof(int32_t);
+        (size_t)maxch * ((w + 8) / 2 + w / 2) * 4 + 2 * (size_t)maxch * GS * GPT * sizeof(int32_t);
     if (smem > RESIDENT_BUDGET) return false;
     auto kern = k_stage1p<T, TH, UP, GS, GPT>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -69,11 +69,21 @@ long cluster_run(const txg_cand *c, long n, double dms, double ddm, double fmax,
 void launch_skzap(const uint8_t *raw, int C_raw, long n0, float thr, unsigned long long *sums,
                   double *stats, uint8_t *mask, cudaStream_t st);
 size_t skzap_max_channels();
-void launch_unpack(const uint8_t *raw, int C_raw, long n0, int td, int fd, float *x, long ldx,
-                   int C, long N, const uint8_t *mask, cudaStream_t st);
-void launch_equalize(float *x, long ldx, int C, long N, uint8_t *live, cudaStream_t st);
-void launch_colmean(const float *x, long ldx, int C, long N, const uint8_t *live, float *out,
-                    cudaStream_t st);
+/* Unpack + downsample.  With `part` (eq_part_tiles(N) x C pairs of 64-bit words) the unpack
+ * also writes equalize's per-tile integer sums; returns whether it did (some unpack shapes
+ * do not, and launch_eq_params then reads the block). */
+long eq_part_tiles(long N);
+bool launch_unpack(const uint8_t *raw, int C_raw, long n0, int td, int fd, float *x, long ldx,
+                   int C, long N, const uint8_t *mask, unsigned long long *part, cudaStream_t st);
+/* equalize: per-channel (mean, 1/sd) and live flags; the apply is fused into the next pass */
+void launch_eq_params(const unsigned long long *part, const float *x, long ldx, int C, long N,
+                      float2 *eqp, uint8_t *live, cudaStream_t st);
+/* x <- standardised x, minus b on live channels when b is given */
+void launch_eq_apply(float *x, long ldx, int C, long N, const float2 *eqp, const float *b,
+                     const uint8_t *live, cudaStream_t st);
+/* column mean (tp: of the standardised block, tp[j] = (mean, 1/sd) of channel j) */
+void launch_colmean(const float *x, long ldx, int C, long N, const uint8_t *live, const float2 *tp,
+                    float *out, cudaStream_t st);
 void launch_smooth(const float *z, long N, long nw, float *b, cudaStream_t st);
 void launch_sub_series(float *x, long ldx, int C, long N, const float *b, const uint8_t *live,
                        cudaStream_t st);
@@ -91,7 +101,8 @@ void launch_kadaneT(float *x, long ldx, int C, long N, int tdk, int fdk, float t
 constexpr int MASK_SEL_WORDS = 2 * 256 + 8;
 void launch_mask(float *x, long ldx, int C, long N, int tdk, int fdk, float thr, float *ds,
                  uint32_t *sel, int32_t *nzap, cudaStream_t st);
-void launch_zdot(float *x, long ldx, int C, long N, float *s, double *sstats,
+/* zp: C (mean, 1/sd) pairs of scratch */
+void launch_zdot(float *x, long ldx, int C, long N, float *s, double *sstats, float2 *zp,
                  cudaStream_t st);
 /* x16: FP16 copy of the channel buffer (same layout, used by the 16-bit precisions, may be
  * null); var: resident launch shape (0 = default; see txg_dedisp.cu). */

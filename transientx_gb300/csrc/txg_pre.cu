@@ -93,11 +93,21 @@ __device__ __forceinline__ double red32(const float *__restrict__ x, const float
     return warp_sum_d(acc);
 }
 
+struct Ident {
+    __device__ __forceinline__ float operator()(float v) const { return v; }
+};
+
+/* v -> (v - m) * inv, the per-channel standardisation of equalize and zdot */
+struct Standardise {
+    float m, inv;
+    __device__ __forceinline__ float operator()(float v) const { return __fmul_rn(__fsub_rn(v, m), inv); }
+};
+
 /* Two fixed-pattern reductions of one row in a single pass (same per-lane order as red32):
- * MODE 1 -> (sum x, sum x*x), MODE 2 -> (sum x, sum x*y). */
-template <int MODE>
+ * MODE 1 -> (sum x, sum x*x), MODE 2 -> (sum x, sum x*y), x = f(stored value). */
+template <int MODE, typename F = Ident>
 __device__ __forceinline__ void red32x2(const float *__restrict__ x, const float *__restrict__ y,
-                                        long n, int lane, double &o1, double &o2)
+                                        long n, int lane, double &o1, double &o2, F f = F())
 {
     double a1 = 0., a2 = 0.;
     long i = lane;
@@ -105,7 +115,7 @@ __device__ __forceinline__ void red32x2(const float *__restrict__ x, const float
         float v[8], q[8];
 #pragma unroll
         for (int r = 0; r < 8; r++) {
-            v[r] = x[i + 32 * r];
+            v[r] = f(x[i + 32 * r]);
             q[r] = MODE == 1 ? v[r] : y[i + 32 * r];
         }
         float r1 = 0.f, r2 = 0.f;
@@ -120,7 +130,7 @@ __device__ __forceinline__ void red32x2(const float *__restrict__ x, const float
     if (i < n) { /* the last, partial run */
         float r1 = 0.f, r2 = 0.f;
         for (; i < n; i += 32) {
-            const float v = x[i];
+            const float v = f(x[i]);
             r1 = __fadd_rn(r1, v);
             r2 = __fadd_rn(r2, MODE == 1 ? __fmul_rn(v, v) : __fmul_rn(v, y[i]));
         }
@@ -135,7 +145,7 @@ __device__ __forceinline__ void red32x2(const float *__restrict__ x, const float
 /* Exact integer sums of (v-128)^p, p = 1..4, per raw channel: threads over channels (4 per
  * thread with 32-bit loads when aligned), time split over blockIdx.y; 64-bit integer atomics
  * make the totals independent of the order. */
-constexpr int SK_TCHUNK = 256;
+constexpr int SK_TCHUNK = 128;
 
 __global__ void __launch_bounds__(256) k_sk_sums(const uint8_t *__restrict__ raw, int C_raw, long n0,
                                                 int vec, unsigned long long *__restrict__ sums)
@@ -145,6 +155,7 @@ __global__ void __launch_bounds__(256) k_sk_sums(const uint8_t *__restrict__ raw
     if (c0 >= C_raw) return;
     const long t0 = (long)blockIdx.y * SK_TCHUNK, t1 = min(t0 + SK_TCHUNK, n0);
     long long a[4][4] = {};
+#pragma unroll 8
     for (long t = t0; t < t1; t++) {
         int v[4];
         if (vec) {
@@ -199,41 +210,85 @@ __global__ void k_sk_stats(const unsigned long long *__restrict__ sums, int C, l
     stats[(size_t)C + c] = ku;
 }
 
-/* One CTA: exact quartiles of skewness and kurtosis by a bitonic sort in shared memory ->
- * mask of channels outside [Q1 - thr*R, Q3 + thr*R] for either statistic. */
-__global__ void __launch_bounds__(1024) k_sk_select(int C, float thr, const double *__restrict__ stats,
-                                                   uint8_t *__restrict__ mask, int P)
+/* Order-preserving 64-bit key of a double (negative values bit-inverted, positive values with
+ * the sign bit set), and its inverse. */
+__device__ __forceinline__ unsigned long long dkey(double v)
 {
-    extern __shared__ double srt[];
+    const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+    return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double dkey_inv(unsigned long long k)
+{
+    return __longlong_as_double((long long)((k >> 63) ? (k & 0x7fffffffffffffffull) : ~k));
+}
+
+/* One CTA: exact quartiles sorted[C/4] and sorted[C-1-C/4] of skewness and kurtosis by a
+ * most-significant-digit radix selection on the order-preserving keys (eight 8-bit passes;
+ * the four selections share each pass) -> mask of channels outside [Q1 - thr*R, Q3 + thr*R]
+ * for either statistic.  Equal values are one value, so the selected quartiles are those of a
+ * sort. */
+__global__ void __launch_bounds__(1024) k_sk_select(int C, float thr, const double *__restrict__ stats,
+                                                   uint8_t *__restrict__ mask)
+{
+    __shared__ unsigned int hist[4][256];
+    __shared__ unsigned long long pref[4];
+    __shared__ unsigned int rank[4];
     __shared__ double lo[2], hi[2];
-    __syncthreads();
-    for (int q = 0; q < 2; q++) {
-        for (int i = threadIdx.x; i < P; i += blockDim.x)
-            srt[i] = i < C ? stats[(size_t)q * C + i] : INFINITY;
+    const int tid = threadIdx.x;
+    if (tid < 4) {
+        pref[tid] = 0ull;
+        rank[tid] = (tid & 1) ? (unsigned)(C - 1 - C / 4) : (unsigned)(C / 4);
+    }
+    for (int shift = 56; shift >= 0; shift -= 8) {
+        for (int e = tid; e < 4 * 256; e += blockDim.x) hist[e >> 8][e & 255] = 0u;
         __syncthreads();
-        for (int k = 2; k <= P; k <<= 1)
-            for (int j = k >> 1; j > 0; j >>= 1) {
-                for (int i = threadIdx.x; i < P; i += blockDim.x) {
-                    const int l = i ^ j;
-                    if (l > i) {
-                        const double x = srt[i], y = srt[l];
-                        const bool up = (i & k) == 0;
-                        if ((x > y) == up) {
-                            srt[i] = y;
-                            srt[l] = x;
-                        }
-                    }
-                }
-                __syncthreads();
+        const unsigned long long hm = shift == 56 ? 0ull : (~0ull << (shift + 8));
+        for (int c = tid; c < 2 * C; c += blockDim.x) {
+            const int q = c >= C;
+            const unsigned long long k = dkey(stats[c]);
+            const unsigned d = (unsigned)(k >> shift) & 255u;
+            if ((k & hm) == pref[2 * q]) atomicAdd(&hist[2 * q][d], 1u);
+            if ((k & hm) == pref[2 * q + 1]) atomicAdd(&hist[2 * q + 1][d], 1u);
+        }
+        __syncthreads();
+        if (tid < 4 * 32) { /* one warp per selection; each lane holds 8 consecutive digits */
+            const int sel = tid >> 5, lane = tid & 31;
+            unsigned cnt[8], tot = 0;
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                cnt[u] = hist[sel][8 * lane + u];
+                tot += cnt[u];
             }
-        if (threadIdx.x == 0) {
-            const double q1 = srt[C / 4], q3 = srt[C - 1 - C / 4];
-            const double R = __dsub_rn(q3, q1);
-            lo[q] = __dsub_rn(q1, __dmul_rn((double)thr, R));
-            hi[q] = __dadd_rn(q3, __dmul_rn((double)thr, R));
+            unsigned incl = tot;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const unsigned y = __shfl_up_sync(FULL, incl, off);
+                if (lane >= off) incl += y;
+            }
+            const unsigned rk = rank[sel], excl = incl - tot;
+            __syncwarp();
+            if (rk >= excl && rk < incl) {
+                unsigned acc = excl;
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    if (rk < acc + cnt[u]) {
+                        pref[sel] |= (unsigned long long)(8 * lane + u) << shift;
+                        rank[sel] = rk - acc;
+                        break;
+                    }
+                    acc += cnt[u];
+                }
+            }
         }
         __syncthreads();
     }
+    if (tid < 2) {
+        const double q1 = dkey_inv(pref[2 * tid]), q3 = dkey_inv(pref[2 * tid + 1]);
+        const double R = __dsub_rn(q3, q1);
+        lo[tid] = __dsub_rn(q1, __dmul_rn((double)thr, R));
+        hi[tid] = __dadd_rn(q3, __dmul_rn((double)thr, R));
+    }
+    __syncthreads();
     for (int c = threadIdx.x; c < C; c += blockDim.x) {
         const double sk = stats[c], ku = stats[(size_t)C + c];
         mask[c] = (sk < lo[0] || sk > hi[0] || ku < lo[1] || ku > hi[1]) ? 1 : 0;
@@ -307,14 +362,18 @@ __global__ void __launch_bounds__(256) k_unpack(const uint8_t *__restrict__ raw,
 /* Unpack for fd | 16 and 16-byte rows: each thread sums, for one output sample, the td raw
  * rows of one 16-channel group (one 16-byte load per row; 16/fd output channels), and a
  * shared-memory transpose gives channel-major coalesced writes.  The sums are of integers
- * below 2^24, exact in FP32, so they equal k_unpack's in any order. */
+ * below 2^24, exact in FP32, so they equal k_unpack's in any order.
+ * With `part`, the CTA also writes, per output channel, the exact integer sums of its 64
+ * values and of their squares (part[(j*gridDim.x + tile)*2 + {0,1}]): equalize's statistics
+ * without another pass over the block. */
 constexpr int UV_BYTES = 128;  /* raw bytes (channels) per CTA row: 8 groups of 16 */
 constexpr int UV_TI = 64;      /* output samples per CTA */
 
 template <int FD>
 __global__ void __launch_bounds__(256) k_unpack_vec(const uint8_t *__restrict__ raw, int C_raw,
                                                    long n0, int td, float *__restrict__ x, long ldx,
-                                                   int C, long N, const uint8_t *__restrict__ mask)
+                                                   int C, long N, const uint8_t *__restrict__ mask,
+                                                   unsigned long long *__restrict__ part)
 {
     constexpr int TJ = UV_BYTES / FD; /* output channels per CTA */
     constexpr int PER = 16 / FD;      /* output channels per thread */
@@ -357,6 +416,34 @@ __global__ void __launch_bounds__(256) k_unpack_vec(const uint8_t *__restrict__ 
         const long i = i0 + ii;
         if (j < C && i < N) x[(long)j * ldx + i] = outt[jj][ii];
     }
+    if (part) {
+        /* samples past N hold 0 and add nothing; values are exact non-negative integers */
+        constexpr int TPC = 256 / TJ, SPT = UV_TI / TPC; /* threads per channel, samples each */
+        __shared__ unsigned long long ps[TPC > 1 ? TPC - 1 : 1][TJ][2];
+        const int jj = threadIdx.x % TJ, pt = threadIdx.x / TJ;
+        unsigned long long a1 = 0ull, a2 = 0ull;
+#pragma unroll 8
+        for (int k = 0; k < SPT; k++) {
+            const unsigned v = __float2uint_rz(outt[jj][pt * SPT + k]);
+            a1 += v;
+            a2 += (unsigned long long)v * v;
+        }
+        if (pt > 0) {
+            ps[pt - 1][jj][0] = a1;
+            ps[pt - 1][jj][1] = a2;
+        }
+        __syncthreads();
+        if (pt == 0 && j0 + jj < C) {
+#pragma unroll
+            for (int p = 0; p < TPC - 1; p++) {
+                a1 += ps[p][jj][0];
+                a2 += ps[p][jj][1];
+            }
+            unsigned long long *o = part + ((size_t)(j0 + jj) * gridDim.x + blockIdx.x) * 2;
+            o[0] = a1;
+            o[1] = a2;
+        }
+    }
 }
 
 /* fallback for large td*fd: one thread per output, no staging */
@@ -378,60 +465,117 @@ __global__ void k_unpack_direct(const uint8_t *__restrict__ raw, int C_raw, int 
 }
 
 /* ---- equalize: exact integer statistics of the integer-valued downsampled block ---------- */
-__global__ void __launch_bounds__(256) k_equalize(float *__restrict__ x, long ldx, int C, long N,
-                                                  uint8_t *__restrict__ live)
+/* Per channel (one warp): the exact sums of the values and of their squares -- from the
+ * unpack's per-tile partial sums when `part` is given, else from the block -- give
+ * mean = s1/N, var = s2/N - mean^2, sd = sqrt(var) (1 when var <= 0) and the standardisation
+ * (v - (float)mean) * (float)(1/sd), stored as eqp[j]; live[j] = var > 0.  The block itself is
+ * standardised later, by whichever pass reads it next. */
+__global__ void __launch_bounds__(256) k_eq_params(const unsigned long long *__restrict__ part,
+                                                   long ntile, const float *__restrict__ x, long ldx,
+                                                   int C, long N, float2 *__restrict__ eqp,
+                                                   uint8_t *__restrict__ live)
 {
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= C) return;
-    float *r = x + (long)w * ldx;
     long long s1 = 0, s2 = 0; /* exact integer sums: any order */
-    long i0 = 0;
-    if ((reinterpret_cast<uintptr_t>(r) & 15) == 0) {
-        const float4 *r4 = reinterpret_cast<const float4 *>(r);
-        const long n4 = N / 4;
-        for (long q = lane; q < n4; q += 32) {
-            const float4 f = r4[q];
-            const long long a = __float2ll_rn(f.x), b = __float2ll_rn(f.y), c = __float2ll_rn(f.z),
-                            d = __float2ll_rn(f.w);
-            s1 += a + b + c + d;
-            s2 += a * a + b * b + c * c + d * d;
+    if (part) {
+        const unsigned long long *p = part + (size_t)w * ntile * 2;
+        for (long t = lane; t < ntile; t += 32) {
+            s1 += (long long)p[2 * t];
+            s2 += (long long)p[2 * t + 1];
         }
-        i0 = 4 * n4;
-    }
-    for (long i = i0 + lane; i < N; i += 32) {
-        long long v = __float2ll_rn(r[i]);
-        s1 += v;
-        s2 += v * v;
+    } else {
+        const float *r = x + (long)w * ldx;
+        long i0 = 0;
+        if ((reinterpret_cast<uintptr_t>(r) & 15) == 0) {
+            const float4 *r4 = reinterpret_cast<const float4 *>(r);
+            const long n4 = N / 4;
+            for (long q = lane; q < n4; q += 32) {
+                const float4 f = r4[q];
+                const long long a = __float2ll_rn(f.x), b = __float2ll_rn(f.y), c = __float2ll_rn(f.z),
+                                d = __float2ll_rn(f.w);
+                s1 += a + b + c + d;
+                s2 += a * a + b * b + c * c + d * d;
+            }
+            i0 = 4 * n4;
+        }
+        for (long i = i0 + lane; i < N; i += 32) {
+            long long v = __float2ll_rn(r[i]);
+            s1 += v;
+            s2 += v * v;
+        }
     }
     s1 = warp_sum_ll(s1);
     s2 = warp_sum_ll(s2);
-    const double dn = (double)N;
-    double mean = __ddiv_rn((double)s1, dn);
-    double var = __dsub_rn(__ddiv_rn((double)s2, dn), __dmul_rn(mean, mean));
-    double sd = var > 0. ? __dsqrt_rn(var) : 1.;
-    const float mf = __double2float_rn(mean), inv = __double2float_rn(__ddiv_rn(1., sd));
-    row_map(r, N, lane, [=](float v, long) { return __fmul_rn(__fsub_rn(v, mf), inv); });
-    if (live && lane == 0) live[w] = var > 0. ? 1 : 0;
+    if (lane == 0) {
+        const double dn = (double)N;
+        double mean = __ddiv_rn((double)s1, dn);
+        double var = __dsub_rn(__ddiv_rn((double)s2, dn), __dmul_rn(mean, mean));
+        double sd = var > 0. ? __dsqrt_rn(var) : 1.;
+        eqp[w] = make_float2(__double2float_rn(mean), __double2float_rn(__ddiv_rn(1., sd)));
+        if (live) live[w] = var > 0. ? 1 : 0;
+    }
+}
+
+/* x[j][i] <- standardise_j(x[j][i]) - b[i] (b null or channel dead: no subtraction): the
+ * equalize apply fused with the baseline subtraction, four samples per thread. */
+__global__ void k_eq_apply(float *__restrict__ x, long ldx, long N, const float2 *__restrict__ eqp,
+                           const float *__restrict__ b, const uint8_t *__restrict__ live)
+{
+    const long i = 4 * ((long)blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = blockIdx.y;
+    if (i >= N) return;
+    const Standardise f{eqp[j].x, eqp[j].y};
+    const float *bb = (b && live[j]) ? b : nullptr;
+    float *r = x + (long)j * ldx;
+    if (i + 3 < N && ((reinterpret_cast<uintptr_t>(r) | reinterpret_cast<uintptr_t>(b)) & 15) == 0) {
+        float4 v = *reinterpret_cast<float4 *>(r + i);
+        v.x = f(v.x);
+        v.y = f(v.y);
+        v.z = f(v.z);
+        v.w = f(v.w);
+        if (bb) {
+            const float4 c = *reinterpret_cast<const float4 *>(bb + i);
+            v.x = __fsub_rn(v.x, c.x);
+            v.y = __fsub_rn(v.y, c.y);
+            v.z = __fsub_rn(v.z, c.z);
+            v.w = __fsub_rn(v.w, c.w);
+        }
+        *reinterpret_cast<float4 *>(r + i) = v;
+    } else {
+        for (long k = i; k < i + 4 && k < N; k++) r[k] = bb ? __fsub_rn(f(r[k]), bb[k]) : f(r[k]);
+    }
 }
 
 /* ---- channel mean per sample (zero-DM series), sequential over channels ---------------- */
 /* Channel sum per sample, in a fixed order: the channels are cut into CSUM_BLK consecutive
  * blocks of ceil(C/CSUM_BLK); each block is summed sequentially from 0.0f (one warp per block,
- * 32 samples per warp) and the block sums are added in block order.  Dead channels are
- * exactly 0, so summing all channels equals summing the live ones; the divisor is the live
- * count when `live` is given (BaseLine) and C otherwise (zdot). */
-constexpr int CSUM_BLK = 8;
+ * 32 samples per warp) and the block sums, empty blocks included, are added in block order.
+ * Dead channels are exactly 0, so summing all channels equals summing the live ones; the
+ * divisor is the live count when `live` is given (BaseLine) and C otherwise (zdot).  With
+ * `tp`, each value is first standardised by its channel's (mean, 1/sd) pair: the column mean
+ * of the standardised block, which is then not stored.  32 blocks keep 32 independent chains
+ * per sample in flight, so short blocks (few CTAs) still cover the GPU. */
+constexpr int CSUM_BLK = 32;
 
+template <bool TP>
 __global__ void __launch_bounds__(32 * CSUM_BLK) k_colmean(const float *__restrict__ x, long ldx, int C,
                                                          long N, const uint8_t *__restrict__ live,
+                                                         const float2 *__restrict__ tp,
                                                          float *__restrict__ out)
 {
-    __shared__ float part[CSUM_BLK][32];
+    __shared__ float part[CSUM_BLK][33];
     __shared__ int nlive_sh;
     const int lane = threadIdx.x, q = threadIdx.y;
     const long i = (long)blockIdx.x * 32 + lane;
     const int cb = (C + CSUM_BLK - 1) / CSUM_BLK;
     const int j0 = q * cb, j1 = min(C, j0 + cb);
+    if (q == 0 && lane == 0) nlive_sh = 0;
+    auto val = [&](float v, int j) {
+        if (!TP) return v;
+        const float2 t = tp[j];
+        return Standardise{t.x, t.y}(v);
+    };
     float acc = 0.f;
     if (i < N) {
         const float *p = x + i;
@@ -441,25 +585,26 @@ __global__ void __launch_bounds__(32 * CSUM_BLK) k_colmean(const float *__restri
 #pragma unroll
             for (int r = 0; r < 16; r++) v[r] = p[(long)(j + r) * ldx];
 #pragma unroll
-            for (int r = 0; r < 16; r++) acc = __fadd_rn(acc, v[r]);
+            for (int r = 0; r < 16; r++) acc = __fadd_rn(acc, val(v[r], j + r));
         }
-        for (; j < j1; j++) acc = __fadd_rn(acc, p[(long)j * ldx]);
+        for (; j < j1; j++) acc = __fadd_rn(acc, val(p[(long)j * ldx], j));
     }
     part[q][lane] = acc;
-    if (q == 0 && lane == 0) {
-        int nl = C;
-        if (live) {
-            nl = 0;
-            for (int c = 0; c < C; c++) nl += live[c];
-        }
-        nlive_sh = nl;
-    }
     __syncthreads();
-    if (q == 0 && i < N) {
-        float t = 0.f;
+    if (live) { /* live channels, counted by the whole CTA */
+        int cnt = 0;
+        for (int c = q * 32 + lane; c < C; c += 32 * CSUM_BLK) cnt += live[c];
 #pragma unroll
+        for (int off = 16; off >= 1; off >>= 1) cnt += __shfl_xor_sync(FULL, cnt, off);
+        if (lane == 0 && cnt) atomicAdd(&nlive_sh, cnt);
+        __syncthreads();
+    }
+    if (q == 0 && i < N) {
+        const int nl = live ? nlive_sh : C;
+        float t = 0.f;
+#pragma unroll 8
         for (int b = 0; b < CSUM_BLK; b++) t = __fadd_rn(t, part[b][lane]);
-        out[i] = nlive_sh > 0 ? __fdiv_rn(t, (float)nlive_sh) : 0.f;
+        out[i] = nl > 0 ? __fdiv_rn(t, (float)nl) : 0.f;
     }
 }
 
@@ -524,14 +669,26 @@ __global__ void k_kadane_ds(const float *__restrict__ x, long ldx, int Cds, long
 /* One thread per downsampled channel runs the maximum-sum scan over the positive and the
  * negated series in one pass (strictly larger sum replaces the best window; the running
  * sum restarts after it drops below zero), then applies the S/N test. */
-constexpr int KS_T = 256; /* samples staged per tile in the kadaneF scan */
+constexpr int KS_T = 96; /* samples per staged tile in the kadaneF scan */
+constexpr int KS_NB = 4; /* tile buffers: three in flight while one is scanned */
+
+__device__ __forceinline__ void cp_async4(float *dst, const float *src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_2() { asm volatile("cp.async.wait_group 2;" ::: "memory"); }
 
 __global__ void __launch_bounds__(32) k_kadane_scan(const float *__restrict__ ds, int Cds, long Nds,
                                                     int tdk, int fdk, float thr, long wnlimit,
                                                     int32_t *__restrict__ ranges)
 {
-    __shared__ float tile[KS_T][33];
-    const int j = blockIdx.x * 32 + threadIdx.x;
+    /* each lane copies (cp.async) and later reads only its own channel's column of the tiles,
+     * so no barrier is needed; a buffer is refilled only after the next tile's scan */
+    __shared__ float tile[KS_NB][KS_T][32];
+    const int lane = threadIdx.x, j = blockIdx.x * 32 + lane;
     float bestp = -INFINITY, bestn = -INFINITY, curp = 0.f, curn = 0.f;
     long csp = 0, csn = 0, sp = 0, ep = -1, sn = 0, en = -1;
     auto step = [&](long i, float v) {
@@ -542,16 +699,31 @@ __global__ void __launch_bounds__(32) k_kadane_scan(const float *__restrict__ ds
         if (curp < 0.f) { curp = 0.f; csp = i + 1; }
         if (curn < 0.f) { curn = 0.f; csn = i + 1; }
     };
-    /* the warp's 32 channels are staged KS_T samples at a time (coalesced rows, all loads in
-     * flight), then each lane scans its channel sequentially */
-    for (long t0 = 0; t0 < Nds; t0 += KS_T) {
-        const int nt = (int)min((long)KS_T, Nds - t0);
-#pragma unroll 16
-        for (int r = 0; r < nt; r++)
-            tile[r][threadIdx.x] = j < Cds ? ds[(t0 + r) * Cds + j] : 0.f;
-        __syncwarp();
-        for (int r = 0; r < nt; r++) step(t0 + r, tile[r][threadIdx.x]);
-        __syncwarp();
+    /* the warp's 32 channels are staged KS_T samples at a time (one coalesced 128-byte row per
+     * copy instruction), then each lane scans its channel sequentially */
+    const long ntl = (Nds + KS_T - 1) / KS_T;
+    auto stage = [&](long tl) {
+        if (tl < ntl && j < Cds) {
+            const long t0 = tl * KS_T;
+            const int nt = (int)min((long)KS_T, Nds - t0);
+            float(*tb)[32] = tile[tl % KS_NB];
+            const float *src = ds + t0 * Cds + j;
+            for (int r = 0; r < nt; r++) cp_async4(&tb[r][lane], src + (long)r * Cds);
+        }
+        cp_async_commit(); /* one group per tile, empty past the end */
+    };
+    stage(0);
+    stage(1);
+    stage(2);
+    for (long tl = 0; tl < ntl; tl++) {
+        cp_async_wait_2(); /* all but the two newest groups done: tile tl has landed */
+        if (j < Cds) {
+            const long t0 = tl * KS_T;
+            const int nt = (int)min((long)KS_T, Nds - t0);
+            const float(*tb)[32] = tile[tl % KS_NB];
+            for (int r = 0; r < nt; r++) step(t0 + r, tb[r][lane]);
+        }
+        stage(tl + 3); /* into the buffer of tile tl-1 */
     }
     if (j >= Cds) return;
     const float var = (float)(tdk * fdk);
@@ -568,15 +740,20 @@ __global__ void __launch_bounds__(32) k_kadane_scan(const float *__restrict__ ds
     }
 }
 
+/* One CTA per channel row: zero its downsampled channel's zapped windows (only those
+ * samples are touched). */
 __global__ void k_kadane_apply(float *__restrict__ x, long ldx, long N, int fdk,
                                const int32_t *__restrict__ ranges)
 {
-    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    int jr = blockIdx.y;
-    if (i >= N) return;
+    const int jr = blockIdx.x;
     const int32_t *r = ranges + 4 * (jr / fdk);
-    if ((r[0] >= 0 && i >= r[0] && i < r[1]) || (r[2] >= 0 && i >= r[2] && i < r[3]))
-        x[(long)jr * ldx + i] = 0.f;
+    float *row = x + (long)jr * ldx;
+#pragma unroll
+    for (int p = 0; p < 2; p++) {
+        const long a = r[2 * p], b = min((long)r[2 * p + 1], N);
+        if (a < 0) continue;
+        for (long i = a + threadIdx.x; i < b; i += blockDim.x) row[i] = 0.f;
+    }
 }
 
 /* ---- kadaneT ---------------------------------------------------------------------------- */
@@ -716,19 +893,24 @@ __global__ void k_mask_apply(float *__restrict__ x, long ldx, long N, int Cds, l
 }
 
 /* ---- zdot ------------------------------------------------------------------------------ */
-__global__ void __launch_bounds__(256) k_zdot_norm(float *__restrict__ x, long ldx, int C, long N)
+/* Per channel (one warp): mean and standard deviation of the row (fixed-pattern sums) ->
+ * zp[j] = ((float)mean, (float)(1/sd)), sd = 1 when the variance is not positive.  The
+ * standardised row is never stored: the channel mean and the fit recompute it. */
+__global__ void __launch_bounds__(256) k_zdot_norm(const float *__restrict__ x, long ldx, int C, long N,
+                                                   float2 *__restrict__ zp)
 {
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= C) return;
-    float *r = x + (long)w * ldx;
+    const float *r = x + (long)w * ldx;
     double s1, s2;
     red32x2<1>(r, nullptr, N, lane, s1, s2);
-    const double dn = (double)N;
-    double mean = __ddiv_rn(s1, dn);
-    double var = __dsub_rn(__ddiv_rn(s2, dn), __dmul_rn(mean, mean));
-    double sd = var > 0. ? __dsqrt_rn(var) : 1.;
-    const float mf = __double2float_rn(mean), inv = __double2float_rn(__ddiv_rn(1., sd));
-    row_map(r, N, lane, [=](float v, long) { return __fmul_rn(__fsub_rn(v, mf), inv); });
+    if (lane == 0) {
+        const double dn = (double)N;
+        double mean = __ddiv_rn(s1, dn);
+        double var = __dsub_rn(__ddiv_rn(s2, dn), __dmul_rn(mean, mean));
+        double sd = var > 0. ? __dsqrt_rn(var) : 1.;
+        zp[w] = make_float2(__double2float_rn(mean), __double2float_rn(__ddiv_rn(1., sd)));
+    }
 }
 
 /* se and ss of the zero-DM series in the fixed pattern of red32x2: lane l's runs of eight
@@ -777,15 +959,19 @@ __global__ void __launch_bounds__(1024) k_zdot_sstats(const float *__restrict__ 
     }
 }
 
+/* Per channel (one warp), on the standardised row n = (x - m)*inv: least-squares alpha, beta
+ * of n on s, then x <- n - (alpha*s + beta). */
 __global__ void __launch_bounds__(256) k_zdot_fit(float *__restrict__ x, long ldx, int C, long N,
+                                                  const float2 *__restrict__ zp,
                                                   const float *__restrict__ s,
                                                   const double *__restrict__ sst)
 {
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= C) return;
     float *r = x + (long)w * ldx;
+    const Standardise nf{zp[w].x, zp[w].y};
     double xe, xs;
-    red32x2<2>(r, s, N, lane, xe, xs);
+    red32x2<2>(r, s, N, lane, xe, xs, nf);
     const double se = sst[0], ss = sst[1], dn = (double)N;
     double tmp = __dsub_rn(__dmul_rn(se, se), __dmul_rn(ss, dn));
     double alpha = 0., beta = 0.;
@@ -794,7 +980,7 @@ __global__ void __launch_bounds__(256) k_zdot_fit(float *__restrict__ x, long ld
         beta = __ddiv_rn(__dsub_rn(__dmul_rn(xs, se), __dmul_rn(xe, ss)), tmp);
     }
     const float af = __double2float_rn(alpha), bf = __double2float_rn(beta);
-    row_map(r, N, lane, [=](float v, long i) { return __fsub_rn(v, __fadd_rn(__fmul_rn(af, s[i]), bf)); });
+    row_map(r, N, lane, [=](float v, long i) { return __fsub_rn(nf(v), __fadd_rn(__fmul_rn(af, s[i]), bf)); });
 }
 
 inline unsigned nblk(long n, int b) { return (unsigned)((n + b - 1) / b); }
@@ -811,20 +997,14 @@ void launch_skzap(const uint8_t *raw, int C_raw, long n0, float thr, unsigned lo
     const long per_thread = vec ? 4 : 1;
     dim3 g1(nblk((C_raw + per_thread - 1) / per_thread, 256), nblk(n0, SK_TCHUNK));
     k_sk_sums<<<g1, 256, 0, st>>>(raw, C_raw, n0, vec, sums);
-    int P = 1;
-    while (P < C_raw) P <<= 1;
-    const size_t smem = (size_t)P * sizeof(double);
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_sk_select, cudaFuncAttributeMaxDynamicSharedMemorySize, 16384 * 8);
-        attr = true;
-    }
     k_sk_stats<<<nblk(C_raw, 256), 256, 0, st>>>(sums, C_raw, n0, stats);
-    k_sk_select<<<1, 1024, smem, st>>>(C_raw, thr, stats, mask, P);
+    k_sk_select<<<1, 1024, 0, st>>>(C_raw, thr, stats, mask);
 }
 
-void launch_unpack(const uint8_t *raw, int C_raw, long n0, int td, int fd, float *x, long ldx,
-                   int C, long N, const uint8_t *mask, cudaStream_t st)
+long eq_part_tiles(long N) { return (long)nblk(N, UV_TI); }
+
+bool launch_unpack(const uint8_t *raw, int C_raw, long n0, int td, int fd, float *x, long ldx,
+                   int C, long N, const uint8_t *mask, unsigned long long *part, cudaStream_t st)
 {
     const bool vec = C_raw % 16 == 0 && (reinterpret_cast<uintptr_t>(raw) & 15) == 0 &&
                      (!mask || (reinterpret_cast<uintptr_t>(mask) & 15) == 0) &&
@@ -832,13 +1012,13 @@ void launch_unpack(const uint8_t *raw, int C_raw, long n0, int td, int fd, float
     if (vec) {
         dim3 grid(nblk(N, UV_TI), nblk(C_raw, UV_BYTES));
         switch (fd) {
-        case 1: k_unpack_vec<1><<<grid, 256, 0, st>>>(raw, C_raw, n0, td, x, ldx, C, N, mask); break;
-        case 2: k_unpack_vec<2><<<grid, 256, 0, st>>>(raw, C_raw, n0, td, x, ldx, C, N, mask); break;
-        case 4: k_unpack_vec<4><<<grid, 256, 0, st>>>(raw, C_raw, n0, td, x, ldx, C, N, mask); break;
-        case 8: k_unpack_vec<8><<<grid, 256, 0, st>>>(raw, C_raw, n0, td, x, ldx, C, N, mask); break;
-        default: k_unpack_vec<16><<<grid, 256, 0, st>>>(raw, C_raw, n0, td, x, ldx, C, N, mask); break;
+        case 1: k_unpack_vec<1><<<grid, 256, 0, st>>>(raw, C_raw, n0, td, x, ldx, C, N, mask, part); break;
+        case 2: k_unpack_vec<2><<<grid, 256, 0, st>>>(raw, C_raw, n0, td, x, ldx, C, N, mask, part); break;
+        case 4: k_unpack_vec<4><<<grid, 256, 0, st>>>(raw, C_raw, n0, td, x, ldx, C, N, mask, part); break;
+        case 8: k_unpack_vec<8><<<grid, 256, 0, st>>>(raw, C_raw, n0, td, x, ldx, C, N, mask, part); break;
+        default: k_unpack_vec<16><<<grid, 256, 0, st>>>(raw, C_raw, n0, td, x, ldx, C, N, mask, part); break;
         }
-        return;
+        return part != nullptr;
     }
     size_t smem = (size_t)UP_TI * td * UP_TJ * fd;
     if (smem <= 96 * 1024) {
@@ -853,17 +1033,29 @@ void launch_unpack(const uint8_t *raw, int C_raw, long n0, int td, int fd, float
         dim3 grid(nblk(N, 128), C);
         k_unpack_direct<<<grid, 128, 0, st>>>(raw, C_raw, td, fd, x, ldx, C, N, mask);
     }
+    return false;
 }
 
-void launch_equalize(float *x, long ldx, int C, long N, uint8_t *live, cudaStream_t st)
+void launch_eq_params(const unsigned long long *part, const float *x, long ldx, int C, long N,
+                      float2 *eqp, uint8_t *live, cudaStream_t st)
 {
-    k_equalize<<<nblk((long)C * 32, 256), 256, 0, st>>>(x, ldx, C, N, live);
+    k_eq_params<<<nblk((long)C * 32, 256), 256, 0, st>>>(part, eq_part_tiles(N), x, ldx, C, N, eqp, live);
 }
 
-void launch_colmean(const float *x, long ldx, int C, long N, const uint8_t *live, float *out,
-                    cudaStream_t st)
+void launch_eq_apply(float *x, long ldx, int C, long N, const float2 *eqp, const float *b,
+                     const uint8_t *live, cudaStream_t st)
 {
-    k_colmean<<<nblk(N, 32), dim3(32, CSUM_BLK), 0, st>>>(x, ldx, C, N, live, out);
+    dim3 grid(nblk((N + 3) / 4, 256), C);
+    k_eq_apply<<<grid, 256, 0, st>>>(x, ldx, N, eqp, b, live);
+}
+
+void launch_colmean(const float *x, long ldx, int C, long N, const uint8_t *live, const float2 *tp,
+                    float *out, cudaStream_t st)
+{
+    if (tp)
+        k_colmean<true><<<nblk(N, 32), dim3(32, CSUM_BLK), 0, st>>>(x, ldx, C, N, live, tp, out);
+    else
+        k_colmean<false><<<nblk(N, 32), dim3(32, CSUM_BLK), 0, st>>>(x, ldx, C, N, live, nullptr, out);
 }
 
 void launch_smooth(const float *z, long N, long nw, float *b, cudaStream_t st)
@@ -897,8 +1089,7 @@ void launch_kadane(float *x, long ldx, int C, long N, int tdk, int fdk, float th
         k_kadane_ds<<<g1, 128, 0, st>>>(x, ldx, Cds, Nds, tdk, fdk, ds);
     }
     k_kadane_scan<<<nblk(Cds, 32), 32, 0, st>>>(ds, Cds, Nds, tdk, fdk, thr, wnlimit, ranges);
-    dim3 g3(nblk(N, 256), Cds * fdk);
-    k_kadane_apply<<<g3, 256, 0, st>>>(x, ldx, N, fdk, ranges);
+    k_kadane_apply<<<Cds * fdk, 128, 0, st>>>(x, ldx, N, fdk, ranges);
 }
 
 void launch_kadaneT(float *x, long ldx, int C, long N, int tdk, int fdk, float thr,
@@ -936,12 +1127,13 @@ void launch_mask(float *x, long ldx, int C, long N, int tdk, int fdk, float thr,
     k_mask_apply<<<g3, 256, 0, st>>>(x, ldx, N, Cds, Nds, tdk, fdk, ds, sel, nzap);
 }
 
-void launch_zdot(float *x, long ldx, int C, long N, float *s, double *sstats, cudaStream_t st)
+void launch_zdot(float *x, long ldx, int C, long N, float *s, double *sstats, float2 *zp,
+                 cudaStream_t st)
 {
-    k_zdot_norm<<<nblk((long)C * 32, 256), 256, 0, st>>>(x, ldx, C, N);
-    k_colmean<<<nblk(N, 32), dim3(32, CSUM_BLK), 0, st>>>(x, ldx, C, N, nullptr, s);
+    k_zdot_norm<<<nblk((long)C * 32, 256), 256, 0, st>>>(x, ldx, C, N, zp);
+    k_colmean<true><<<nblk(N, 32), dim3(32, CSUM_BLK), 0, st>>>(x, ldx, C, N, nullptr, zp, s);
     k_zdot_sstats<<<1, 1024, 0, st>>>(s, N, sstats);
-    k_zdot_fit<<<nblk((long)C * 32, 256), 256, 0, st>>>(x, ldx, C, N, s, sstats);
+    k_zdot_fit<<<nblk((long)C * 32, 256), 256, 0, st>>>(x, ldx, C, N, zp, s, sstats);
 }
 
 } // namespace txg
