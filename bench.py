@@ -321,9 +321,13 @@ def run_ours(args, wl):
                       precision=args.precision, flags=tx.FLAG_CLUSTER, zapthre=ZAPTHRE)
         hpin = host.numpy()
 
-        def pop_all(st):
+        def pop_all(st, wait=True):
+            # while streaming, only blocks whose clustering is done are popped (a streaming
+            # consumer polls; the pushing thread never waits on host clustering)
             for r in range(len(wl.rows)):
                 while True:
+                    if not wait and not s.result_ready(r):
+                        break
                     out = s.pop_result(r, points=False)
                     if out is None:
                         break
@@ -336,7 +340,7 @@ def run_ours(args, wl):
         def step_host(st):
             for b in range(nblk):
                 s.push_block(hpin[b * wl.ndump:(b + 1) * wl.ndump])
-                pop_all(st)
+                pop_all(st, wait=False)
             s.sync(allow_overflow=True)
             pop_all(st)
 
@@ -353,7 +357,9 @@ def run_ours(args, wl):
                "h2d_bytes_per_step": nblk * blk_bytes,
                "d2h_bytes_per_step": st["d2h"] // max(1, args.steps),
                "clusters_per_step": st["clusters"] / max(1, args.steps),
-               "includes": "H2D from pinned host memory, candidate read-back, Cluster::run per block"}
+               "includes": "H2D from pinned host memory, candidate read-back, Cluster::run per "
+                           "block, every block's results popped (as they become ready, the rest "
+                           "after the step's sync)"}
         s.close()
 
     if rank != 0:

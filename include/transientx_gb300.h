@@ -161,6 +161,12 @@ typedef struct {
 int txg_pop_result(txg_handle *h, int32_t beam, int32_t row, txg_result *res, txg_cand *points,
                    int64_t pcap, txg_cand *clusters, int64_t ccap);
 
+/* Whether txg_pop_result would return at once: *ready = 1 when the oldest waiting block of
+ * (beam,row) has its points sorted and clustered, 0 while a worker thread is still on it.
+ * Returns TXG_ERR_STATE when no block is waiting.  No reference counterpart: a streaming
+ * caller polls with it so that the thread pushing blocks never waits on host clustering. */
+int txg_result_ready(txg_handle *h, int32_t beam, int32_t row, int32_t *ready);
+
 /* Dense Boxcar::mxS / mxwn of the last block (plan flag TXG_FLAG_DENSE): [ndm][nsamples]. */
 int txg_get_dense(txg_handle *h, int32_t beam, int32_t row, float *mxS, int32_t *mxwn);
 

@@ -100,3 +100,23 @@ def test_boxcar_segmented_equals_single_cta(tx, oracle, n, monkeypatch):
             np.testing.assert_array_equal(W1, W2)
             np.testing.assert_array_equal(np.sort(c1, order=["idm", "isamp"]),
                                           np.sort(c2, order=["idm", "isamp"]))
+
+
+@pytest.mark.parametrize("n", [3000, 62496])
+def test_boxcar_candidates_same_with_and_without_dense(tx, oracle, n):
+    """Without dense output the search keeps only the largest S per sample and finds the width
+    of each point above the threshold afterwards: the candidate list equals the tracked
+    search's bit for bit (single-CTA and segmented rows, moment and IQR statistics)."""
+    rng = np.random.default_rng(n + 3)
+    tim = rng.normal(0, 20, (12, n)).astype(np.float32)
+    tim[3, n // 4: n // 4 + 30] += 300
+    tim[7, n - 20:] += 500
+    tim[9, :50] += 400
+    tim[11] = 5.0
+    vwn = oracle.width_ladder(1e-4, 0.02, 0.1, 64e-6)
+    key = ["idm", "isamp"]
+    for iqr in (False, True):
+        _, _, c1 = tx.boxcar(tim, vwn, iqr=iqr, thre=3.0)
+        _, _, c2 = tx.boxcar(tim, vwn, iqr=iqr, thre=3.0, dense=False)
+        assert len(c1) > 100
+        np.testing.assert_array_equal(np.sort(c1, order=key), np.sort(c2, order=key))

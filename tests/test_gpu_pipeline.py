@@ -119,6 +119,25 @@ def test_rfi_options_match_oracle(tx, oracle, name):
             assert fired.get(op[0], 0) > 0, (name, op, fired)
 
 
+def test_zdot_long_rows_match_oracle(tx, oracle):
+    """Long blocks (45056 samples, zdot only): the preprocessed block equals the oracle's bit
+    for bit."""
+    from transientx_gb300 import SinglePulse, synth
+    C, ndump = 32, 45056
+    f = synth.band(C, 1500.0, 1200.0)
+    fil = synth.Filterbank(C, 64e-6, f, 2 * ndump, 5, sines=[(3, 20.0, 0.01, 0.5)])
+    rows = [SinglePulse(td=1, fd=1, dms=0.0, ddm=1.0, ndm=8, maxw=0.01, rfilist=[["zdot"]],
+                        bswidth=0.05)]
+    orow = oracle_rows(oracle, rows, fil, ndump, tx)[0]
+    with tx.Search(rows, C, fil.tsamp, f, ndump, flags=tx.FLAG_KEEP_SERIES, zapthre=4.0) as s:
+        for b in range(2):
+            raw = fil.generate(b * ndump, ndump)
+            s.push_block(raw)
+            s.sync()
+            orow.run(raw)
+            np.testing.assert_array_equal(s.block(0), orow.block(), err_msg=f"block {b}")
+
+
 @pytest.mark.parametrize("nchans,td,fd", [(128, 1, 1), (128, 3, 2), (256, 2, 16), (100, 2, 5),
                                           (96, 4, 3)])
 def test_unpack_paths_match_oracle(tx, oracle, nchans, td, fd):
@@ -216,6 +235,29 @@ def test_reduced_precision_series(tx, prec, bound):
             scale = ta.std(axis=1, keepdims=True)
             err = np.abs(ta - tb) / scale
             assert err.max() < bound, (prec, r, err.max())
+
+
+def test_result_ready_polls_without_waiting(tx):
+    """txg_result_ready: None with nothing waiting; after sync every waiting block is ready and
+    pops in push order with the same results as a blocking pop."""
+    fil, rows, ndump = small_workload()
+    with tx.Search(rows, fil.nchans, fil.tsamp, fil.freqs, ndump, flags=tx.FLAG_CLUSTER) as s:
+        assert s.result_ready(0) is None
+        n = fil.nsamples // ndump
+        for b in range(n):
+            s.push_block(fil.generate(b * ndump, ndump))
+            while s.result_ready(0):
+                s.pop_result(0)
+        s.sync()
+        counters = []
+        while True:
+            r = s.result_ready(0)
+            if r is None:
+                break
+            assert r is True
+            counters.append(s.pop_result(0)[0].counter)
+        assert counters == sorted(counters) and len(counters) >= 1
+        assert s.pop_result(0) is None
 
 
 def test_candidate_overflow_is_reported(tx):

@@ -105,7 +105,7 @@ EXPORTS = [
     "txg_get_block", "txg_get_zap_ranges", "txg_get_tables", "txg_width_ladder", "txg_boxcar",
     "txg_cluster", "txg_get_timing", "txg_get_stream", "txg_strerror", "txg_version",
     "txg_describe_row", "txg_pop_result", "txg_get_mask", "txg_kadaneF_noalloc",
-    "txg_get_subdata", "txg_cand_band", "txg_replot", "txg_get_timdata_q",
+    "txg_get_subdata", "txg_cand_band", "txg_replot", "txg_get_timdata_q", "txg_result_ready",
 ]
 
 _lib: Optional[C.CDLL] = None
@@ -157,6 +157,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
                                       C.c_float, C.c_int64, vp, vp]
     L.txg_pop_result.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(txg_result), vp, C.c_int64,
                                  vp, C.c_int64]
+    L.txg_result_ready.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(C.c_int32)]
     L.txg_describe_row.argtypes = [C.POINTER(txg_plan), C.c_int32, C.POINTER(txg_row_info), vp,
                                    vp, vp, vp]
     _lib = L
@@ -392,6 +393,17 @@ class Search:
         if rc not in (OK, ERR_OVERFLOW):
             _check(rc, "candidates")
         return out
+
+    def result_ready(self, row: int = 0, beam: int = 0) -> Optional[bool]:
+        """Whether pop_result would return without waiting on host clustering; None when no
+        block of (beam,row) is waiting."""
+        L = load_library()
+        ready = C.c_int32(0)
+        rc = L.txg_result_ready(self.h, beam, row, C.byref(ready))
+        if rc == ERR_STATE:
+            return None
+        _check(rc)
+        return bool(ready.value)
 
     def pop_result(self, row: int = 0, beam: int = 0, points: bool = True):
         """Oldest unread block of (beam,row) as (result, points, clusters), or None.  Clusters

@@ -149,6 +149,11 @@ struct Workers {
         std::unique_lock<std::mutex> lk(m);
         done.wait(lk, [&] { return r.ready; });
     }
+    bool is_ready(const Result &r)
+    {
+        std::lock_guard<std::mutex> lk(m);
+        return r.ready;
+    }
     void drain()
     {
         std::unique_lock<std::mutex> lk(m);
@@ -926,6 +931,18 @@ int txg_pop_result(txg_handle *h, int32_t beam, int32_t row, txg_result *res, tx
         if (m > 0) memcpy(clusters, r.clusters.data(), m * sizeof(txg_cand));
     }
     return result_status(h, r);
+}
+
+int txg_result_ready(txg_handle *h, int32_t beam, int32_t row, int32_t *ready)
+{
+    int rc = check_beam_row(h, beam, row);
+    if (rc) return rc;
+    if (!ready) return fail(TXG_ERR_ARG, "null output");
+    BeamRow &b = h->br[beam][row];
+    *ready = 0;
+    if (b.fifo.empty()) return fail(TXG_ERR_STATE, "no block result waiting");
+    *ready = h->pool->is_ready(*b.fifo.front()) ? 1 : 0;
+    return TXG_OK;
 }
 
 int txg_get_dense(txg_handle *h, int32_t beam, int32_t row, float *mxS, int32_t *mxwn)

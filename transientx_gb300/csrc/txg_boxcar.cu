@@ -23,7 +23,9 @@ namespace txg {
 namespace {
 
 constexpr int BX_THREADS = 512;
-constexpr int BX_U = 4; /* samples per thread per pass: width parameters loaded once for all */
+constexpr int BX_U = 4;  /* samples per thread per pass, tracked search: width parameters
+                          * loaded once for all */
+constexpr int BX_UF = 8; /* the same for the maximum-only search */
 constexpr unsigned FULL = 0xffffffffu;
 constexpr size_t BX_SMEM_MAX = 200 * 1024; /* + ~10 KB static stays under 227 KB */
 
@@ -92,10 +94,10 @@ __device__ float select_kth(const float *row, long n, long k, unsigned *hist)
     return fkey_inv(prefix);
 }
 
-/* Best S over the width ladder for BX_U samples i = i0 + u*BX_THREADS.  CHECK selects the
- * per-width range test (needed near the row ends); AVX2 reproduces the unordered-compare blend
- * of the -mavx2 build. */
-template <bool CHECK, bool AVX2>
+/* Best S over the width ladder for U samples i = i0 + u*BX_THREADS, with its width (later
+ * widths win ties).  CHECK selects the per-width range test (needed near the row ends); AVX2
+ * reproduces the unordered-compare blend of the -mavx2 build. */
+template <bool CHECK, bool AVX2, int U>
 __device__ __forceinline__ void widths_pass(const float *__restrict__ c, int coff, int i0, int iend,
                                             int nw, const int4 *__restrict__ wpar,
                                             const float *__restrict__ temp_w, float *best, int *bw)
@@ -105,7 +107,7 @@ __device__ __forceinline__ void widths_pass(const float *__restrict__ c, int cof
         const int4 p = wpar[w];
         const float tw = temp_w[w];
 #pragma unroll
-        for (int u = 0; u < BX_U; u++) {
+        for (int u = 0; u < U; u++) {
             const int i = i0 + u * BX_THREADS;
             if (!CHECK || (i >= p.x && i < p.z && i < iend)) {
                 const float S = __fmul_rn(__fsub_rn(c[i - coff + p.y], c[i - coff - p.x]), tw);
@@ -121,7 +123,96 @@ __device__ __forceinline__ void widths_pass(const float *__restrict__ c, int cof
     }
 }
 
-template <bool AVX2>
+/* The same search keeping only the best S (S is never NaN: var > 0 and the sums are finite,
+ * so the maximum is that of the tracked search). */
+template <bool CHECK, int U>
+__device__ __forceinline__ void widths_max(const float *__restrict__ c, int coff, int i0, int iend,
+                                           int nw, const int4 *__restrict__ wpar,
+                                           const float *__restrict__ temp_w, float *best)
+{
+    for (int w = 0; w < nw; w++) {
+        const int4 p = wpar[w];
+        const float tw = temp_w[w];
+        const int hz = min(p.z, iend);
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int i = i0 + u * BX_THREADS;
+            if (!CHECK || (i >= p.x && i < hz)) {
+                const float S = __fmul_rn(__fsub_rn(c[i - coff + p.y], c[i - coff - p.x]), tw);
+                best[u] = fmaxf(best[u], S);
+            }
+        }
+    }
+}
+
+/* Width search over samples [s_lo, iend) of row k, the running sum at c[j - coff]; every
+ * width is in range for samples in [lo_all, hi_all).  Points with S > thre are appended to
+ * the candidate list (warp-aggregated atomic), dense mxS/mxwn written when given.  TRACK keeps
+ * the best width at every step (the dense output and the AVX2 blend need it); otherwise the
+ * pass keeps only the maximum S and the width of each point above the threshold comes from
+ * the tracked search of that one sample -- the same comparisons in the same order. */
+template <bool AVX2, bool TRACK>
+__device__ __forceinline__ void search_row(const float *__restrict__ c, int coff, int s_lo, int iend,
+                                           int lo_all, int hi_all, int nw, const int4 *__restrict__ wpar,
+                                           const float *__restrict__ temp_w, bool active, float thre,
+                                           long k, long n, txg_cand *__restrict__ cand,
+                                           int *__restrict__ ncand, long cap, float *__restrict__ mxS,
+                                           int32_t *__restrict__ mxwn)
+{
+    constexpr int U = TRACK ? BX_U : BX_UF;
+    const int tid = threadIdx.x, lane = tid & 31;
+    for (int base = s_lo; base < iend; base += BX_THREADS * U) {
+        float best[U];
+        int bw[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            best[u] = 0.f;
+            bw[u] = 0;
+        }
+        if (active) {
+            const int i0 = base + tid;
+            const bool inner = base >= lo_all && base + BX_THREADS * U <= hi_all && base + BX_THREADS * U <= iend;
+            if (TRACK) {
+                if (inner)
+                    widths_pass<false, AVX2, U>(c, coff, i0, iend, nw, wpar, temp_w, best, bw);
+                else
+                    widths_pass<true, AVX2, U>(c, coff, i0, iend, nw, wpar, temp_w, best, bw);
+            } else {
+                if (inner)
+                    widths_max<false, U>(c, coff, i0, iend, nw, wpar, temp_w, best);
+                else
+                    widths_max<true, U>(c, coff, i0, iend, nw, wpar, temp_w, best);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int i = base + tid + u * BX_THREADS;
+            if (TRACK && i < iend && mxS) {
+                mxS[k * n + i] = best[u];
+                mxwn[k * n + i] = bw[u];
+            }
+            const bool hit = i < iend && best[u] > thre;
+            if (!TRACK && hit) {
+                float b1 = 0.f;
+                int w1 = 0;
+                widths_pass<true, false, 1>(c, coff, i, iend, nw, wpar, temp_w, &b1, &w1);
+                bw[u] = w1;
+            }
+            const unsigned m = __ballot_sync(FULL, hit);
+            if (m) {
+                int basei = 0;
+                if (lane == __ffs(m) - 1) basei = atomicAdd(ncand, __popc(m));
+                basei = __shfl_sync(FULL, basei, __ffs(m) - 1);
+                if (hit) {
+                    const long slot = basei + __popc(m & ((1u << lane) - 1u));
+                    if (slot < cap) cand[slot] = txg_cand{(int32_t)k, (int32_t)i, bw[u], best[u]};
+                }
+            }
+        }
+    }
+}
+
+template <bool AVX2, bool TRACK>
 __global__ void __launch_bounds__(BX_THREADS)
 k_boxcar(const float *__restrict__ tim, long ldt, long n, const int32_t *__restrict__ vwn,
          int nw, int iqr, float thre, txg_cand *__restrict__ cand,
@@ -242,44 +333,8 @@ k_boxcar(const float *__restrict__ tim, long ldt, long n, const int32_t *__restr
     }
     __syncthreads();
 
-    const bool active = var > 0.f;
-    const int lane = tid & 31;
-    const int nn = (int)n;
-    for (int base = 0; base < nn; base += BX_THREADS * BX_U) {
-        float best[BX_U];
-        int bw[BX_U];
-#pragma unroll
-        for (int u = 0; u < BX_U; u++) {
-            best[u] = 0.f;
-            bw[u] = 0;
-        }
-        if (active) {
-            const int i0 = base + tid;
-            if (base >= lo_all && base + BX_THREADS * BX_U <= hi_all)
-                widths_pass<false, AVX2>(c, 0, i0, nn, nw, wpar, temp_w, best, bw);
-            else
-                widths_pass<true, AVX2>(c, 0, i0, nn, nw, wpar, temp_w, best, bw);
-        }
-#pragma unroll
-        for (int u = 0; u < BX_U; u++) {
-            const int i = base + tid + u * BX_THREADS;
-            if (i < nn && mxS) {
-                mxS[k * n + i] = best[u];
-                mxwn[k * n + i] = bw[u];
-            }
-            const bool hit = i < nn && best[u] > thre;
-            const unsigned m = __ballot_sync(FULL, hit);
-            if (m) {
-                int basei = 0;
-                if (lane == __ffs(m) - 1) basei = atomicAdd(ncand, __popc(m));
-                basei = __shfl_sync(FULL, basei, __ffs(m) - 1);
-                if (hit) {
-                    const long slot = basei + __popc(m & ((1u << lane) - 1u));
-                    if (slot < cap) cand[slot] = txg_cand{(int32_t)k, (int32_t)i, bw[u], best[u]};
-                }
-            }
-        }
-    }
+    search_row<AVX2, TRACK>(c, 0, 0, (int)n, lo_all, hi_all, nw, wpar, temp_w, var > 0.f, thre, k, n,
+                            cand, ncand, cap, mxS, mxwn);
 }
 
 /* ---- rows longer than one CTA's shared memory ------------------------------------------ */
@@ -373,7 +428,7 @@ k_boxcar_prep(const float *__restrict__ tim, long ldt, long n, int iqr, double *
     }
 }
 
-template <bool AVX2>
+template <bool AVX2, bool TRACK>
 __global__ void __launch_bounds__(BX_THREADS)
 k_boxcar_seg(const float *__restrict__ tim, long ldt, long n, const int32_t *__restrict__ vwn,
              int nw, float thre, const double *__restrict__ scratch, txg_cand *__restrict__ cand,
@@ -435,44 +490,8 @@ k_boxcar_seg(const float *__restrict__ tim, long ldt, long n, const int32_t *__r
     }
     __syncthreads();
 
-    const bool active = var > 0.f;
-    const int lane = tid & 31;
-    const int coff = (int)h_lo, iend = (int)s_hi;
-    for (int base = (int)s_lo; base < iend; base += BX_THREADS * BX_U) {
-        float best[BX_U];
-        int bw[BX_U];
-#pragma unroll
-        for (int u = 0; u < BX_U; u++) {
-            best[u] = 0.f;
-            bw[u] = 0;
-        }
-        if (active) {
-            const int i0 = base + tid;
-            if (base >= lo_all && base + BX_THREADS * BX_U <= hi_all && base + BX_THREADS * BX_U <= iend)
-                widths_pass<false, AVX2>(c, coff, i0, iend, nw, wpar, temp_w, best, bw);
-            else
-                widths_pass<true, AVX2>(c, coff, i0, iend, nw, wpar, temp_w, best, bw);
-        }
-#pragma unroll
-        for (int u = 0; u < BX_U; u++) {
-            const int i = base + tid + u * BX_THREADS;
-            if (i < iend && mxS) {
-                mxS[k * n + i] = best[u];
-                mxwn[k * n + i] = bw[u];
-            }
-            const bool hit = i < iend && best[u] > thre;
-            const unsigned m = __ballot_sync(FULL, hit);
-            if (m) {
-                int basei = 0;
-                if (lane == __ffs(m) - 1) basei = atomicAdd(ncand, __popc(m));
-                basei = __shfl_sync(FULL, basei, __ffs(m) - 1);
-                if (hit) {
-                    const long slot = basei + __popc(m & ((1u << lane) - 1u));
-                    if (slot < cap) cand[slot] = txg_cand{(int32_t)k, (int32_t)i, bw[u], best[u]};
-                }
-            }
-        }
-    }
+    search_row<AVX2, TRACK>(c, (int)h_lo, (int)s_lo, (int)s_hi, lo_all, hi_all, nw, wpar, temp_w,
+                            var > 0.f, thre, k, n, cand, ncand, cap, mxS, mxwn);
 }
 
 } // namespace
@@ -505,15 +524,19 @@ int launch_boxcar(const float *tim, long ldt, long ndm, long n, const int32_t *v
     if (nw > 256 || n >= (1L << 31)) return TXG_ERR_UNSUPPORTED;
     if ((size_t)n <= boxcar_max_samples() && !(force_segmented() && scratch)) {
         size_t smem = (size_t)n * sizeof(float);
-        if (avx2_tail) {
-            cudaFuncSetAttribute(k_boxcar<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BX_SMEM_MAX);
-            k_boxcar<true><<<(unsigned)ndm, BX_THREADS, smem, st>>>(tim, ldt, n, vwn, nw, iqr, thre, cand,
-                                                                    ncand, cap, mxS, mxwn);
-        } else {
-            cudaFuncSetAttribute(k_boxcar<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BX_SMEM_MAX);
-            k_boxcar<false><<<(unsigned)ndm, BX_THREADS, smem, st>>>(tim, ldt, n, vwn, nw, iqr, thre, cand,
-                                                                     ncand, cap, mxS, mxwn);
-        }
+#define TXG_BX(A, T)                                                                                  \
+    do {                                                                                              \
+        cudaFuncSetAttribute(k_boxcar<A, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BX_SMEM_MAX); \
+        k_boxcar<A, T><<<(unsigned)ndm, BX_THREADS, smem, st>>>(tim, ldt, n, vwn, nw, iqr, thre, cand, ncand, \
+                                                                 cap, mxS, mxwn);                      \
+    } while (0)
+        if (avx2_tail)
+            TXG_BX(true, true);
+        else if (mxS)
+            TXG_BX(false, true);
+        else
+            TXG_BX(false, false);
+#undef TXG_BX
         return TXG_OK;
     }
     /* long rows: statistics and chunk offsets per row, then segments of SEG_CHUNKS chunks */
@@ -525,15 +548,19 @@ int launch_boxcar(const float *tim, long ldt, long ndm, long n, const int32_t *v
     if (smem > BX_SMEM_MAX || nseg > 65535) return TXG_ERR_UNSUPPORTED;
     k_boxcar_prep<<<(unsigned)ndm, BX_THREADS, 0, st>>>(tim, ldt, n, iqr, scratch);
     dim3 grid((unsigned)ndm, (unsigned)nseg);
-    if (avx2_tail) {
-        cudaFuncSetAttribute(k_boxcar_seg<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_boxcar_seg<true><<<grid, BX_THREADS, smem, st>>>(tim, ldt, n, vwn, nw, thre, scratch, cand,
-                                                           ncand, cap, mxS, mxwn);
-    } else {
-        cudaFuncSetAttribute(k_boxcar_seg<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_boxcar_seg<false><<<grid, BX_THREADS, smem, st>>>(tim, ldt, n, vwn, nw, thre, scratch, cand,
-                                                            ncand, cap, mxS, mxwn);
-    }
+#define TXG_BXS(A, T)                                                                                 \
+    do {                                                                                              \
+        cudaFuncSetAttribute(k_boxcar_seg<A, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+        k_boxcar_seg<A, T><<<grid, BX_THREADS, smem, st>>>(tim, ldt, n, vwn, nw, thre, scratch, cand, ncand, \
+                                                            cap, mxS, mxwn);                           \
+    } while (0)
+    if (avx2_tail)
+        TXG_BXS(true, true);
+    else if (mxS)
+        TXG_BXS(false, true);
+    else
+        TXG_BXS(false, false);
+#undef TXG_BXS
     return TXG_OK;
 }
 
