@@ -805,13 +805,19 @@ static void stage1_chunked(const float *xh, long ldh, long col0, int C, long N, 
 }
 
 /* Resident launch shapes (threads per set x samples per thread, thread sets x groups each):
- *   FP32 windows: 0 = 256x2 4x8 (default), 1 = 256x2 1x16, 2 = 512x1 1x16, 3 = 256x2 2x8,
- *                 4 = 256x2 2x16, 5 = 256x1 2x8, 6 = 256x2 4x4
- *   16-bit pairs: 0 = 128x2 4x8 (default), 1 = 256x1 1x16, 2 = 256x1 2x8, 3 = 256x1 2x16,
- *                 4 = 256x1 4x4, 5 = 128x1 4x8, 6 = 256x1 4x8
- * (measured on the 4096-channel workload: more warps per SM over the same resident window
- * pay until the per-thread delay loads dominate).  A shape whose windows do not fit falls back
- * to 1x16, then to the chunked kernel. */
+ *   FP32 windows: 0 = 32x16 16x4 (default), 1 = 256x2 1x16, 2 = 512x1 1x16, 3 = 256x2 2x8,
+ *                 4 = 256x2 2x16, 5 = 256x1 2x8, 6 = 256x2 4x4, 7 = 128x4 4x8, 8 = 256x4 2x8,
+ *                 9 = 128x4 2x8, 10 = 128x4 8x4, 11 = 64x8 8x4, 12 = 64x8 4x4, 13 = 64x8 16x4,
+ *                 14 = 64x8 8x8, 15 = 64x16 8x4, 16 = 256x2 4x8, 17 = 32x8 16x8
+ *   16-bit pairs: 0 = 32x8 16x4 (default), 1 = 256x1 1x16, 2 = 256x1 2x8, 3 = 256x1 2x16,
+ *                 4 = 256x1 4x4, 5 = 128x1 4x8, 6 = 256x1 4x8, 7 = 64x4 8x4, 8 = 128x2 8x4,
+ *                 9 = 64x4 16x4, 10 = 128x2 4x8, 11 = 64x8 8x4
+ * Every channel step loads the thread's delays (broadcast 16-byte loads, two shared-memory
+ * wavefronts each) and then one window element per sample per group: many samples per thread
+ * and one warp per set keep the delay loads a small share of the shared-memory traffic
+ * (measured on the 4096-channel workload: 32x16 16x4 took stage 1 from 185 to 159 ms per 20
+ * blocks against 256x2 4x8).  A shape whose windows do not fit falls back to 256x2 1x16, then
+ * to the chunked kernel. */
 template <typename T>
 static void stage1_dispatch(const float *xh, const __half *x16, long ldh, long col0, int C, long N,
                             int nsub, int ng, const int32_t *sub_start, const int32_t *d1, long maxd1,
@@ -830,7 +836,12 @@ static void stage1_dispatch(const float *xh, const __half *x16, long ldh, long c
             case 4: done = stage1p_try<T, 256, 1, 4, 4>(TXG_PARGS); break;
             case 5: done = stage1p_try<T, 128, 1, 4, 8>(TXG_PARGS); break;
             case 6: done = stage1p_try<T, 256, 1, 4, 8>(TXG_PARGS); break;
-            default: done = stage1p_try<T, 128, 2, 4, 8>(TXG_PARGS); break;
+            case 7: done = stage1p_try<T, 64, 4, 8, 4>(TXG_PARGS); break;
+            case 8: done = stage1p_try<T, 128, 2, 8, 4>(TXG_PARGS); break;
+            case 9: done = stage1p_try<T, 64, 4, 16, 4>(TXG_PARGS); break;
+            case 10: done = stage1p_try<T, 128, 2, 4, 8>(TXG_PARGS); break;
+            case 11: done = stage1p_try<T, 64, 8, 8, 4>(TXG_PARGS); break;
+            default: done = stage1p_try<T, 32, 8, 16, 4>(TXG_PARGS); break;
             }
             if (!done) done = stage1p_try<T, 256, 1, 1, 16>(TXG_PARGS);
         }
@@ -842,7 +853,18 @@ static void stage1_dispatch(const float *xh, const __half *x16, long ldh, long c
         case 4: done = stage1r_try<T, 256, 2, 2, 16>(TXG_ARGS); break;
         case 5: done = stage1r_try<T, 256, 1, 2, 8>(TXG_ARGS); break;
         case 6: done = stage1r_try<T, 256, 2, 4, 4>(TXG_ARGS); break;
-        default: done = stage1r_try<T, 256, 2, 4, 8>(TXG_ARGS); break;
+        case 7: done = stage1r_try<T, 128, 4, 4, 8>(TXG_ARGS); break;
+        case 8: done = stage1r_try<T, 256, 4, 2, 8>(TXG_ARGS); break;
+        case 9: done = stage1r_try<T, 128, 4, 2, 8>(TXG_ARGS); break;
+        case 10: done = stage1r_try<T, 128, 4, 8, 4>(TXG_ARGS); break;
+        case 11: done = stage1r_try<T, 64, 8, 8, 4>(TXG_ARGS); break;
+        case 12: done = stage1r_try<T, 64, 8, 4, 4>(TXG_ARGS); break;
+        case 13: done = stage1r_try<T, 64, 8, 16, 4>(TXG_ARGS); break;
+        case 14: done = stage1r_try<T, 64, 8, 8, 8>(TXG_ARGS); break;
+        case 15: done = stage1r_try<T, 64, 16, 8, 4>(TXG_ARGS); break;
+        case 16: done = stage1r_try<T, 256, 2, 4, 8>(TXG_ARGS); break;
+        case 17: done = stage1r_try<T, 32, 8, 16, 8>(TXG_ARGS); break;
+        default: done = stage1r_try<T, 32, 16, 16, 4>(TXG_ARGS); break;
         }
     }
     if (!done) done = stage1r_try<T, 256, 2, 1, 16>(TXG_ARGS);
