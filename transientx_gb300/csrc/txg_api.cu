@@ -533,7 +533,7 @@ int run_block(txg_handle *h, int beam, const uint8_t *raw)
         if (gated) {
             const long t0 = counter - P.N - P.offset;
             launch_stage2(b.ring, P.R, P.nsub, P.G, P.cfg.ndm, P.nout, D.d2, P.s2_span,
-                          pmod(t0, P.R), h->prec, P.s2_kb, b.tim, P.nout, sl.dcount + 1, h->st);
+                          pmod(t0, P.R), h->prec, P.s2_var, P.s2_kb, b.tim, P.nout, sl.dcount + 1, h->st);
             TXG_CUDA_TRY(cudaGetLastError());
             if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[4], h->st));
             rc = launch_boxcar(b.tim, P.nout, P.cfg.ndm, P.nout, D.vwn, (int)P.vwn.size(), P.maxwn,
@@ -589,11 +589,12 @@ int finish_plan(RowPlan &P, int r)
      * most 1024 samples) plus the largest within-subband delay plus alignment and one pair
      * element, so it may read up to H + N + 1040 columns: pad the pitch past that */
     P.ldh = ((P.H + P.N + 1056) + 31) / 32 * 32;
-    /* launch shapes; TXG_DEDISP_SHAPE="s1=<variant>,s2kb=<KB>" overrides them */
+    /* launch shapes; TXG_DEDISP_SHAPE="s1=<variant>,s2=<variant>,s2kb=<KB>" overrides them */
     if (const char *e = getenv("TXG_DEDISP_SHAPE")) {
         int v = 0;
         if (const char *q = strstr(e, "s1=")) P.s1_var = (sscanf(q + 3, "%d", &v) == 1) ? v : P.s1_var;
-        if (const char *q = strstr(e, "s2kb=")) P.s2_kb = (sscanf(q + 5, "%d", &v) == 1 && v >= 16 && v <= 200) ? v : P.s2_kb;
+        if (const char *q = strstr(e, "s2kb=")) P.s2_kb = (sscanf(q + 5, "%d", &v) == 1 && v >= 8 && v <= 200) ? v : P.s2_kb;
+        if (const char *q = strstr(e, "s2=")) P.s2_var = (sscanf(q + 3, "%d", &v) == 1) ? v : P.s2_var;
     }
     if (P.vwn.size() > 256) return fail(TXG_ERR_UNSUPPORTED, "more than 256 boxcar widths");
     if (!boxcar_supported(P.nout, P.maxwn, (int)P.vwn.size()))

@@ -476,16 +476,18 @@ constexpr int S2_THREADS = 128;
 constexpr int S2_U = 2;                  /* samples per thread */
 constexpr int S2_TT = S2_THREADS * S2_U;
 
-/* grid: x = time tiles, y = (group, DM chunk of KPC).  Shared memory: for a chunk of `sc`
+/* grid: x = time tiles, y = (group, DM chunk of KPC); TH threads take U samples each of the
+ * S2_TT-sample tile.  Shared memory: for a chunk of `sc`
  * subbands their ring windows (each S2_TT + d2[klast][s] - d2[kfirst][s] plus alignment),
  * then the d2 offsets [sc][KPC] and the window bookkeeping.  Each output adds its subbands
  * in ascending order from 0.0f. */
-template <typename T, int KPC>
-__global__ void __launch_bounds__(S2_THREADS)
+template <typename T, int KPC, int TH, int U>
+__global__ void __launch_bounds__(TH)
 k_stage2(const T *__restrict__ ring, long R, int nsub, int G, long ndm, long nout,
          const int32_t *__restrict__ d2, long t0_mod, int sc, long wtot_max,
          float *__restrict__ tim, long ldt, int *err)
 {
+    static_assert(TH * U == S2_TT && TH >= 32, "the tile is S2_TT samples");
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ __align__(8) uint64_t bar;
     T *win = reinterpret_cast<T *>(smraw);
@@ -507,23 +509,23 @@ k_stage2(const T *__restrict__ ring, long R, int nsub, int G, long ndm, long nou
     }
     __syncthreads();
 
-    float acc[KPC][S2_U];
+    float acc[KPC][U];
 #pragma unroll
     for (int k = 0; k < KPC; k++)
 #pragma unroll
-        for (int q = 0; q < S2_U; q++) acc[k][q] = 0.f;
+        for (int q = 0; q < U; q++) acc[k][q] = 0.f;
 
     uint32_t phase = 0;
     constexpr int EPC = 16 / (int)sizeof(T); /* elements per 16 bytes */
     for (int s0 = 0; s0 < nsub; s0 += sc) {
         const int sn = min(sc, nsub - s0);
-        for (int e = tid; e < sn * KPC; e += S2_THREADS) {
+        for (int e = tid; e < sn * KPC; e += TH) {
             const int ss = e / KPC, k = e % KPC;
             const int lo = d2[(size_t)k0 * nsub + s0 + ss];
             doff[e] = d2[(size_t)(k0 + (k < kn ? k : kn - 1)) * nsub + s0 + ss] - lo;
         }
         /* window of each subband: ring start rounded down to 16 bytes, length, offset */
-        for (int ss = tid; ss < sn; ss += S2_THREADS) {
+        for (int ss = tid; ss < sn; ss += TH) {
             const int s = s0 + ss;
             const long lo = d2[(size_t)k0 * nsub + s];
             const long hi = d2[(size_t)(k0 + kn - 1) * nsub + s];
@@ -555,7 +557,7 @@ k_stage2(const T *__restrict__ ring, long R, int nsub, int G, long ndm, long nou
             }
         }
         __syncthreads();
-        for (int ss = tid; ss < sn; ss += S2_THREADS) {
+        for (int ss = tid; ss < sn; ss += TH) {
             const T *row = ring + ((size_t)g * nsub + s0 + ss) * R;
             const long pos = wpos[ss], len = wlen[ss], tstart = wts[ss];
             wbeg[ss] = (int32_t)(pos + wal[ss]);
@@ -592,8 +594,8 @@ k_stage2(const T *__restrict__ ring, long R, int nsub, int G, long ndm, long nou
 #pragma unroll
             for (int k = 0; k < KPC; k++)
 #pragma unroll
-                for (int q = 0; q < S2_U; q++)
-                    acc[k][q] = __fadd_rn(acc[k][q], to_f(wr[dd[k] + q * S2_THREADS]));
+                for (int q = 0; q < U; q++)
+                    acc[k][q] = __fadd_rn(acc[k][q], to_f(wr[dd[k] + q * TH]));
         }
         __syncthreads();
     }
@@ -601,8 +603,8 @@ k_stage2(const T *__restrict__ ring, long R, int nsub, int G, long ndm, long nou
     for (int k = 0; k < KPC; k++) {
         if (k < kn) {
 #pragma unroll
-            for (int q = 0; q < S2_U; q++) {
-                const long u = u0 + tid + q * S2_THREADS;
+            for (int q = 0; q < U; q++) {
+                const long u = u0 + tid + q * TH;
                 if (u < nout) tim[(k0 + k) * ldt + u] = acc[k][q];
             }
         }
@@ -612,13 +614,14 @@ k_stage2(const T *__restrict__ ring, long R, int nsub, int G, long ndm, long nou
 /* Stage 2 on a 16-bit ring, two consecutive samples per 32-bit shared-memory load: the
  * subband windows are held as even-aligned pairs (bulk copies) and odd-aligned pairs (built
  * in shared memory).  Same order of additions as k_stage2. */
-template <typename T, int KPC, int TH>
+template <typename T, int KPC, int TH, int UP>
 __global__ void __launch_bounds__(TH)
 k_stage2p(const T *__restrict__ ring, long R, int nsub, int G, long ndm, long nout,
           const int32_t *__restrict__ d2, long t0_mod, int sc, long wtot_max,
           float *__restrict__ tim, long ldt, int *err)
 {
-    constexpr int TT = 2 * TH;
+    constexpr int TT = 2 * TH * UP;
+    static_assert(TT == S2_TT && TH >= 32, "the tile is S2_TT samples");
     constexpr int EPC = 8; /* 16-bit elements per 16 bytes */
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ __align__(8) uint64_t bar;
@@ -644,9 +647,11 @@ k_stage2p(const T *__restrict__ ring, long R, int nsub, int G, long ndm, long no
     }
     __syncthreads();
 
-    float acc[KPC][2];
+    float acc[KPC][2 * UP];
 #pragma unroll
-    for (int k = 0; k < KPC; k++) acc[k][0] = acc[k][1] = 0.f;
+    for (int k = 0; k < KPC; k++)
+#pragma unroll
+        for (int q = 0; q < 2 * UP; q++) acc[k][q] = 0.f;
 
     uint32_t phase = 0;
     for (int s0 = 0; s0 < nsub; s0 += sc) {
@@ -726,7 +731,9 @@ k_stage2p(const T *__restrict__ ring, long R, int nsub, int G, long ndm, long no
                 dd[4 * kq + 3] = d.w;
             }
 #pragma unroll
-            for (int k = 0; k < KPC; k++) addp(acc[k][0], acc[k][1], wr[dd[k]], T());
+            for (int k = 0; k < KPC; k++)
+#pragma unroll
+                for (int q = 0; q < UP; q++) addp(acc[k][2 * q], acc[k][2 * q + 1], wr[dd[k] + q * TH], T());
         }
         __syncthreads();
     }
@@ -734,8 +741,8 @@ k_stage2p(const T *__restrict__ ring, long R, int nsub, int G, long ndm, long no
     for (int k = 0; k < KPC; k++) {
         if (k < kn) {
 #pragma unroll
-            for (int q = 0; q < 2; q++) {
-                const long u = u0 + 2 * tid + q;
+            for (int q = 0; q < 2 * UP; q++) {
+                const long u = u0 + 2 * (tid + (q >> 1) * TH) + (q & 1);
                 if (u < nout) tim[(k0 + k) * ldt + u] = acc[k][q];
             }
         }
@@ -987,7 +994,7 @@ void launch_cand_vpf(const void *ring, long R, int nsub, int G, const int32_t *d
 /* Ring length a stage-2 window may need (the ring must be longer, so a window wraps once). */
 long stage2_window(long span) { return (long)S2_TT + span + 16; }
 
-template <typename T, int KPC>
+template <typename T, int KPC, int TH>
 static void stage2_impl(const void *ring, long R, int nsub, int G, long ndm, long nout,
                         const int32_t *d2, long span, long t0_mod, float *tim, long ldt, size_t budget,
                         int *err, cudaStream_t st)
@@ -1003,19 +1010,20 @@ static void stage2_impl(const void *ring, long R, int nsub, int G, long ndm, lon
     const int nkc = (G + KPC - 1) / KPC;
     const long ng = (ndm + G - 1) / G;
     dim3 grid(nblk(nout, S2_TT), (unsigned)(ng * nkc));
-    cudaFuncSetAttribute(k_stage2<T, KPC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_stage2<T, KPC><<<grid, S2_THREADS, smem, st>>>((const T *)ring, R, nsub, G, ndm, nout, d2,
-                                                     t0_mod, sc, wtot, tim, ldt, err);
+    auto kern = k_stage2<T, KPC, TH, S2_TT / TH>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<grid, TH, smem, st>>>((const T *)ring, R, nsub, G, ndm, nout, d2, t0_mod, sc, wtot, tim, ldt,
+                                 err);
 }
 
-/* 16-bit ring: pair kernel, TT = 2 * 128 samples (the FP32 tile), windows doubled by the odd
- * copy. */
-template <typename T, int KPC>
+/* 16-bit ring: pair kernel, TH threads of UP pairs over the S2_TT-sample tile, windows doubled
+ * by the odd copy. */
+template <typename T, int KPC, int TH>
 static void stage2p_impl(const void *ring, long R, int nsub, int G, long ndm, long nout,
                          const int32_t *d2, long span, long t0_mod, float *tim, long ldt, size_t budget,
                          int *err, cudaStream_t st)
 {
-    constexpr int TH = S2_TT / 2;
+    constexpr int UP = S2_TT / 2 / TH;
     const long wlen = ((long)S2_TT + span + 2 + 7 + 7) / 8 * 8; /* halves */
     const size_t per = wlen * 4 + KPC * sizeof(int32_t) + 4 * sizeof(int32_t);
     int sc = (int)((budget - 80) / per);
@@ -1027,21 +1035,63 @@ static void stage2p_impl(const void *ring, long R, int nsub, int G, long ndm, lo
     const int nkc = (G + KPC - 1) / KPC;
     const long ng = (ndm + G - 1) / G;
     dim3 grid(nblk(nout, S2_TT), (unsigned)(ng * nkc));
-    cudaFuncSetAttribute(k_stage2p<T, KPC, TH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_stage2p<T, KPC, TH><<<grid, TH, smem, st>>>((const T *)ring, R, nsub, G, ndm, nout, d2, t0_mod,
-                                                  sc, wtot, tim, ldt, err);
+    auto kern = k_stage2p<T, KPC, TH, UP>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<grid, TH, smem, st>>>((const T *)ring, R, nsub, G, ndm, nout, d2, t0_mod, sc, wtot, tim, ldt,
+                                 err);
+}
+
+/* FP32 threads per CTA by variant: 0 = 32 (8 samples each; DM chunks wider than 16 take 64),
+ * 1 = 64 (4), 2 = 128 (2).  Fewer threads with more samples each load the per-subband delays
+ * (broadcast 16-byte loads) for more additions: on the 4096-channel workload variant 0 with
+ * 18 KB per CTA took stage 2 from 91 to 81 ms per 20 blocks against 128 threads with 36 KB. */
+template <typename T, int K>
+static void stage2_var(int var, const void *ring, long R, int nsub, int G, long ndm, long nout,
+                       const int32_t *d2, long span, long t0_mod, float *tim, long ldt, size_t budget,
+                       int *err, cudaStream_t st)
+{
+    if constexpr (K <= 16) {
+        if (var == 0) {
+            stage2_impl<T, K, 32>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, budget, err, st);
+            return;
+        }
+    }
+    if (var == 2)
+        stage2_impl<T, K, 128>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, budget, err, st);
+    else
+        stage2_impl<T, K, 64>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, budget, err, st);
+}
+
+/* 16-bit pair kernel by variant: 0 = 32 threads of 4 pairs (DM chunks wider than 16: 64 of
+ * 2), 1 = 64 of 2, 2 = 128 of 1 (variant 0 with 18 KB per CTA: 71 -> 65 ms per 20 blocks of
+ * the 4096-channel workload against variant 2 with 36 KB). */
+template <typename T, int K>
+static void stage2p_var(int var, const void *ring, long R, int nsub, int G, long ndm, long nout,
+                        const int32_t *d2, long span, long t0_mod, float *tim, long ldt, size_t budget,
+                        int *err, cudaStream_t st)
+{
+    if constexpr (K <= 16) {
+        if (var == 0) {
+            stage2p_impl<T, K, 32>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, budget, err, st);
+            return;
+        }
+    }
+    if (var == 2)
+        stage2p_impl<T, K, 128>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, budget, err, st);
+    else
+        stage2p_impl<T, K, 64>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, budget, err, st);
 }
 
 template <typename T, bool PAIRS>
-static void stage2_dispatch(const void *ring, long R, int nsub, int G, long ndm, long nout,
+static void stage2_dispatch(int var, const void *ring, long R, int nsub, int G, long ndm, long nout,
                             const int32_t *d2, long span, long t0_mod, float *tim, long ldt,
                             size_t budget, int *err, cudaStream_t st)
 {
 #define TXG_S2(K)                                                                                   \
     if constexpr (PAIRS)                                                                            \
-        stage2p_impl<T, K>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, budget, err, st); \
+        stage2p_var<T, K>(var, ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, budget, err, st); \
     else                                                                                            \
-        stage2_impl<T, K>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, budget, err, st)
+        stage2_var<T, K>(var, ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, budget, err, st)
     switch (stage2_kpc(G)) {
     case 8: TXG_S2(8); break;
     case 16: TXG_S2(16); break;
@@ -1052,16 +1102,20 @@ static void stage2_dispatch(const void *ring, long R, int nsub, int G, long ndm,
 }
 
 void launch_stage2(const void *ring, long R, int nsub, int G, long ndm, long nout,
-                   const int32_t *d2, long span, long t0_mod, int prec, int s2_kb, float *tim,
-                   long ldt, int *err, cudaStream_t st)
+                   const int32_t *d2, long span, long t0_mod, int prec, int s2_var, int s2_kb,
+                   float *tim, long ldt, int *err, cudaStream_t st)
 {
-    const size_t budget = (size_t)(s2_kb >= 16 ? s2_kb : 36) * 1024;
+    /* s2_kb 0: 18 KB per CTA (one-warp CTAs, about twelve per SM) */
+    const size_t budget = (size_t)(s2_kb >= 8 ? s2_kb : 18) * 1024;
     if (prec == TXG_PREC_BF16)
-        stage2_dispatch<__nv_bfloat16, true>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, budget, err, st);
+        stage2_dispatch<__nv_bfloat16, true>(s2_var, ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt,
+                                             budget, err, st);
     else if (prec == TXG_PREC_FP16)
-        stage2_dispatch<__half, true>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, budget, err, st);
+        stage2_dispatch<__half, true>(s2_var, ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, budget,
+                                      err, st);
     else
-        stage2_dispatch<float, false>(ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, budget, err, st);
+        stage2_dispatch<float, false>(s2_var, ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, budget,
+                                      err, st);
 }
 
 } // namespace txg

@@ -48,7 +48,8 @@ struct RowPlan {
     float mask_thr = 0.f;      /* threMask (IQR units) */
     /* dedispersion launch shapes */
     int s1_var = 0;   /* resident stage-1 launch shape, 0 = default */
-    int s2_kb = 36;   /* stage-2 shared memory per CTA, KB (36: six CTAs per SM) */
+    int s2_var = 0;   /* stage-2 threads per CTA, 0 = default (see txg_dedisp.cu) */
+    int s2_kb = 0;    /* stage-2 shared memory per CTA, KB (0 = the kernel's default) */
 };
 
 /* Deterministic planning helpers (txg_plan.cpp). */
@@ -113,10 +114,11 @@ void launch_stage1(const float *xh, const __half *x16, long ldh, long col0, int 
 void launch_to_half(const float *x, long ldh, int C, long ncols, __half *y, cudaStream_t st);
 long stage2_span(const int32_t *d2h, int nsub, int G, long ndm);
 long stage2_window(long span);
-/* s2_kb: shared-memory budget of one stage-2 CTA in KB (CTAs per SM follow from it) */
+/* s2_var: FP32 threads per CTA (0 = 32, 1 = 64, 2 = 128); s2_kb: shared-memory budget of
+ * one stage-2 CTA in KB, 0 = the kernel's default (CTAs per SM follow from it) */
 void launch_stage2(const void *ring, long R, int nsub, int G, long ndm, long nout,
-                   const int32_t *d2, long span, long t0_mod, int prec, int s2_kb, float *tim,
-                   long ldt, int *err, cudaStream_t st);
+                   const int32_t *d2, long span, long t0_mod, int prec, int s2_var, int s2_kb,
+                   float *tim, long ldt, int *err, cudaStream_t st);
 /* the subband series of fine DM k ([nsub][nout] floats) and, per candidate, the per-subband
  * sums over its window (vpf [n][nsub]) from the subband ring */
 void launch_subdata(const void *ring, long R, int nsub, int G, const int32_t *d2, long k,
