@@ -28,8 +28,8 @@ sys.path.insert(0, ROOT)
 ELEM = {"fp32": 4, "bf16": 2, "fp16": 2}
 # DRAM read+write bytes per launch of the dominant class from one ncu capture of this workload
 # (profiles/traffic_nchan4096_n2M_rfi_dm3000.md: mean over the three ddplan rows' launches)
-PROFILED_TRAFFIC = {("nchan4096_n2M_rfi_dm3000", "fp32", "stage1"): 1270.6e6,
-                    ("nchan4096_n2M_rfi_dm3000", "fp16", "stage1"): 608.4e6}
+PROFILED_TRAFFIC = {("nchan4096_n2M_rfi_dm3000", "fp32", "stage1"): 1285.2e6,
+                    ("nchan4096_n2M_rfi_dm3000", "fp16", "stage1"): 607.5e6}
 ZAPTHRE = 4.0  # PreprocessLite skewness/kurtosis channel-zap threshold (transientx_fil default)
 
 
@@ -121,6 +121,21 @@ def class_bytes(info, sp, nchans_raw, ndump_raw, ncand, elem):
 
 RFI_LAUNCHES = {"kadaneF": 3, "kadaneT": 3, "zdot": 4, "zero": 2, "mask": 10}
 BOXCAR_ROW_MAX = 51200  # samples of a dedispersed row one boxcar CTA holds; longer rows: 2 kernels
+
+
+SMEM_BYTES_PER_CLK = 128  # shared-memory bytes one SM delivers per clock
+NSM = 152
+
+
+def class_smem_bytes(info, elem):
+    """Shared-memory bytes a perfect implementation must load for one launch of the classes
+    bound by shared memory: stage 1 loads one window element per addition (C x ngroup x N
+    additions), stage 2 likewise (nsub x ndm x (N + noverlap)), the boxcar two running-sum
+    values per (sample, width).  Other classes: None."""
+    N, C = info.ndump, info.nchans
+    return [None, None, float(elem) * C * info.ngroup * N,
+            float(elem) * info.nsub * info.ndm * info.nsamples,
+            8.0 * info.ndm * info.nsamples * info.nwidths]
 
 
 def launches_per_block(sp, info, gated, precision="fp32"):
@@ -299,6 +314,11 @@ def run_ours(args, wl):
         cb = class_bytes(info, sp, fil.nchans, wl.ndump, ncand_avg, ELEM[args.precision])
         for c in range(5):
             nb_total[c] += cb[c] * (args.steps * nblk if c < 3 else nblocks_r)
+    sm_total = [0.0] * 5
+    for r, (sp, info) in enumerate(zip(wl.rows, infos)):
+        sb = class_smem_bytes(info, ELEM[args.precision])
+        for c in (2, 3, 4):
+            sm_total[c] += sb[c] * (args.steps * nblk if c < 3 else stats["gated"][r])
     peak, peak_kind = measured_peaks()
     achieved = nb_total[top] / (cls_ms[top] / 1e3) / 1e9
     roof = {"bound": "hbm", "kernel": names[top], "achieved": achieved, "peak": peak,
@@ -311,6 +331,15 @@ def run_ours(args, wl):
             "class_launches": {names[c]: int(cls_n[c]) for c in range(5)},
             "class_algorithmic_GBps": {names[c]: (nb_total[c] / (cls_ms[c] / 1e3) / 1e9
                                                    if cls_ms[c] > 0 else None) for c in range(5)}}
+    if top in (2, 3, 4) and cls_ms[top] > 0:
+        # the dedispersion and boxcar kernels are bound by shared-memory bandwidth, not HBM
+        sm_clk = (clk or {}).get("sm_mhz") or 2070.0
+        sm_peak = NSM * SMEM_BYTES_PER_CLK * sm_clk * 1e6 / 1e12
+        sm_ach = sm_total[top] / (cls_ms[top] / 1e3) / 1e12
+        roof["smem"] = {"achieved": sm_ach, "peak": sm_peak, "unit": "TB/s", "frac": sm_ach / sm_peak,
+                        "peak_basis": f"{NSM} SMs x {SMEM_BYTES_PER_CLK} B/clock x median SM clock",
+                        "basis": "one shared-memory window element per addition (stages 1, 2), "
+                                 "two running-sum loads per sample and width (boxcar)"}
 
     s.close()
     e2e = None

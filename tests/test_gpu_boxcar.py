@@ -116,7 +116,8 @@ def test_boxcar_candidates_same_with_and_without_dense(tx, oracle, n):
     vwn = oracle.width_ladder(1e-4, 0.02, 0.1, 64e-6)
     key = ["idm", "isamp"]
     for iqr in (False, True):
-        _, _, c1 = tx.boxcar(tim, vwn, iqr=iqr, thre=3.0)
-        _, _, c2 = tx.boxcar(tim, vwn, iqr=iqr, thre=3.0, dense=False)
-        assert len(c1) > 100
-        np.testing.assert_array_equal(np.sort(c1, order=key), np.sort(c2, order=key))
+        for thre in (3.0, -1.0):  # a negative threshold keeps every sample, S = 0 ones included
+            _, _, c1 = tx.boxcar(tim, vwn, iqr=iqr, thre=thre)
+            _, _, c2 = tx.boxcar(tim, vwn, iqr=iqr, thre=thre, dense=False)
+            assert len(c1) > 100
+            np.testing.assert_array_equal(np.sort(c1, order=key), np.sort(c2, order=key))

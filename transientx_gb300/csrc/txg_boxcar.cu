@@ -149,8 +149,8 @@ __device__ __forceinline__ void widths_max(const float *__restrict__ c, int coff
  * width is in range for samples in [lo_all, hi_all).  Points with S > thre are appended to
  * the candidate list (warp-aggregated atomic), dense mxS/mxwn written when given.  TRACK keeps
  * the best width at every step (the dense output and the AVX2 blend need it); otherwise the
- * pass keeps only the maximum S and the width of each point above the threshold comes from
- * the tracked search of that one sample -- the same comparisons in the same order. */
+ * pass keeps only the maximum S and the width of each point above the threshold is found
+ * afterwards with the same arithmetic. */
 template <bool AVX2, bool TRACK>
 __device__ __forceinline__ void search_row(const float *__restrict__ c, int coff, int s_lo, int iend,
                                            int lo_all, int hi_all, int nw, const int4 *__restrict__ wpar,
@@ -192,11 +192,31 @@ __device__ __forceinline__ void search_row(const float *__restrict__ c, int coff
                 mxwn[k * n + i] = bw[u];
             }
             const bool hit = i < iend && best[u] > thre;
-            if (!TRACK && hit) {
-                float b1 = 0.f;
-                int w1 = 0;
-                widths_pass<true, false, 1>(c, coff, i, iend, nw, wpar, temp_w, &b1, &w1);
-                bw[u] = w1;
+            if (!TRACK) {
+                /* the tracked search keeps the last width whose S reaches the final best (>= with
+                 * best starting at 0): the largest w with S_w == best, or width 0 when none
+                 * equals it (best stayed 0).  The warp finds it for each hit in turn, one width
+                 * per lane, with the same arithmetic as the search. */
+                unsigned hm = __ballot_sync(FULL, hit);
+                while (hm) {
+                    const int src = __ffs(hm) - 1;
+                    hm &= hm - 1;
+                    const int is = __shfl_sync(FULL, i, src);
+                    const float bs = __shfl_sync(FULL, best[u], src);
+                    int wf = -1;
+                    for (int w0 = 0; w0 < nw; w0 += 32) {
+                        const int w = w0 + lane;
+                        bool eq = false;
+                        if (w < nw) {
+                            const int4 p = wpar[w];
+                            if (is >= p.x && is < min(p.z, iend))
+                                eq = __fmul_rn(__fsub_rn(c[is - coff + p.y], c[is - coff - p.x]), temp_w[w]) == bs;
+                        }
+                        const unsigned e = __ballot_sync(FULL, eq);
+                        if (e) wf = w0 + 31 - __clz(e);
+                    }
+                    if (lane == src) bw[u] = wf >= 0 ? wpar[wf].w : 0;
+                }
             }
             const unsigned m = __ballot_sync(FULL, hit);
             if (m) {
