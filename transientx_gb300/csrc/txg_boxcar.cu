@@ -233,7 +233,7 @@ __device__ __forceinline__ void search_row(const float *__restrict__ c, int coff
 }
 
 template <bool AVX2, bool TRACK>
-__global__ void __launch_bounds__(BX_THREADS)
+__global__ void __launch_bounds__(BX_THREADS, 4)
 k_boxcar(const float *__restrict__ tim, long ldt, long n, const int32_t *__restrict__ vwn,
          int nw, int iqr, float thre, txg_cand *__restrict__ cand,
          int *__restrict__ ncand, long cap, float *__restrict__ mxS, int32_t *__restrict__ mxwn)
@@ -297,13 +297,8 @@ k_boxcar(const float *__restrict__ tim, long ldt, long n, const int32_t *__restr
     __syncthreads();
     if (tid < 32) { /* exclusive scan of the chunk totals in FP64 by one warp */
         const int per = BX_THREADS / 32;
-        double v[BX_THREADS / 32];
         double run = 0.;
-#pragma unroll
-        for (int q = 0; q < per; q++) {
-            v[q] = chunk_off[tid * per + q];
-            run = __dadd_rn(run, v[q]);
-        }
+        for (int q = 0; q < per; q++) run = __dadd_rn(run, chunk_off[tid * per + q]);
         double incl = run;
 #pragma unroll
         for (int off = 1; off < 32; off <<= 1) {
@@ -313,10 +308,10 @@ k_boxcar(const float *__restrict__ tim, long ldt, long n, const int32_t *__restr
         /* exclusive prefix = the left neighbour's inclusive sum */
         const double left = __shfl_up_sync(FULL, incl, 1);
         double ex = tid == 0 ? 0. : left;
-#pragma unroll
         for (int q = 0; q < per; q++) {
+            const double v = chunk_off[tid * per + q];
             chunk_off[tid * per + q] = ex;
-            ex = __dadd_rn(ex, v[q]);
+            ex = __dadd_rn(ex, v);
         }
     }
     __syncthreads();
@@ -417,13 +412,8 @@ k_boxcar_prep(const float *__restrict__ tim, long ldt, long n, int iqr, double *
     __syncthreads();
     if (tid < 32) {
         const int per = BX_THREADS / 32;
-        double v[BX_THREADS / 32];
         double run = 0.;
-#pragma unroll
-        for (int q = 0; q < per; q++) {
-            v[q] = chunk_off[tid * per + q];
-            run = __dadd_rn(run, v[q]);
-        }
+        for (int q = 0; q < per; q++) run = __dadd_rn(run, chunk_off[tid * per + q]);
         double incl = run;
 #pragma unroll
         for (int off = 1; off < 32; off <<= 1) {
@@ -432,10 +422,10 @@ k_boxcar_prep(const float *__restrict__ tim, long ldt, long n, int iqr, double *
         }
         const double left = __shfl_up_sync(FULL, incl, 1);
         double ex = tid == 0 ? 0. : left;
-#pragma unroll
         for (int q = 0; q < per; q++) {
+            const double v = chunk_off[tid * per + q];
             chunk_off[tid * per + q] = ex;
-            ex = __dadd_rn(ex, v[q]);
+            ex = __dadd_rn(ex, v);
         }
     }
     __syncthreads();
