@@ -824,13 +824,19 @@ static void stage1_chunked(const float *xh, long ldh, long col0, int C, long N, 
  * and one warp per set keep the delay loads a small share of the shared-memory traffic
  * (measured on the 4096-channel workload: 32x16 16x4 took stage 1 from 185 to 159 ms per 20
  * blocks against 256x2 4x8).  A shape whose windows do not fit falls back to 256x2 1x16, then
- * to the chunked kernel. */
+ * to the chunked kernel (any negative variant selects the chunked kernel directly).  The
+ * 16-bit fallbacks past the pair kernels read the FP32 block (one rounding fewer than the FP16
+ * copy), so their series can differ in the last bits from the pair kernels'. */
 template <typename T>
 static void stage1_dispatch(const float *xh, const __half *x16, long ldh, long col0, int C, long N,
                             int nsub, int ng, const int32_t *sub_start, const int32_t *d1, long maxd1,
                             int maxch, T *ring, long R, long tbase_mod, int var, int *err,
                             cudaStream_t st)
 {
+    if (var < 0) { /* the chunked kernel, whatever fits */
+        stage1_chunked<T>(xh, ldh, col0, C, N, nsub, ng, sub_start, d1, maxd1, maxch, ring, R, tbase_mod, err, st);
+        return;
+    }
     bool done = false;
 #define TXG_ARGS xh, ldh, col0, C, N, nsub, ng, sub_start, d1, maxd1, maxch, ring, R, tbase_mod, err, st
 #define TXG_PARGS x16, ldh, col0, C, N, nsub, ng, sub_start, d1, maxd1, maxch, ring, R, tbase_mod, err, st
