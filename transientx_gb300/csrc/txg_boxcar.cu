@@ -5,7 +5,8 @@
  *
  * One CTA per DM row.  The row is staged in shared memory, its mean/variance reduced
  * (FP32 runs combined in FP64), then the running sum of (x - mean) is formed in place by a
- * block scan (per-thread FP32 chunks, FP64 chunk offsets) and every sample i keeps the
+ * block scan (per-thread FP32 chunks, FP64 chunk offsets added as a float pair) and every
+ * sample i keeps the
  * largest S = (c[i+wh] - c[i-wl]) * sqrt(1/(wn*var)) over the width ladder, later widths
  * winning ties (S >= best, best starting at 0) as in boxcar.cpp:253-262.  Rows with
  * var <= 0 yield zeros (boxcar.cpp:242).  The IQR statistics (boxcar.cpp:215-227) come from
@@ -316,11 +317,14 @@ k_boxcar(const float *__restrict__ tim, long ldt, long n, const int32_t *__restr
     }
     __syncthreads();
     {
+        /* the chunk's FP64 offset as a float pair: c[i] = (hi + run) + lo, two FP32 adds per
+         * sample (the FP64 pipe is a small fraction of the FP32 one on this part) */
         const double off = chunk_off[tid];
+        const float oh = __double2float_rn(off), ol = __double2float_rn(__dsub_rn(off, (double)oh));
         float run = 0.f;
         for (long i = a; i < b; i++) {
             run = __fadd_rn(run, __fsub_rn(c[i], mean));
-            c[i] = __double2float_rn(__dadd_rn(off, (double)run));
+            c[i] = __fadd_rn(__fadd_rn(oh, run), ol);
         }
     }
     for (int w = tid; w < nw; w += BX_THREADS) {
@@ -355,7 +359,8 @@ k_boxcar(const float *__restrict__ tim, long ldt, long n, const int32_t *__restr
 /* ---- rows longer than one CTA's shared memory ------------------------------------------ */
 /* The single-CTA kernel's arithmetic depends only on n: statistics by the fixed run pattern,
  * and the running sum over BX_THREADS chunks of L = ceil(n/BX_THREADS) samples (FP32 inside a
- * chunk, FP64 chunk offsets).  k_boxcar_prep computes, per row, the same statistics and chunk
+ * chunk, FP64 chunk offsets added as a float pair).  k_boxcar_prep computes, per row, the same
+ * statistics and chunk
  * offsets from global memory; k_boxcar_seg rebuilds the running sum of a segment of chunks
  * plus a halo of the widest boxcar and runs the same width passes: results are identical to
  * k_boxcar's.  scratch row k: [0, BX_THREADS) chunk offsets, [BX_THREADS] mean and var. */
@@ -492,10 +497,11 @@ k_boxcar_seg(const float *__restrict__ tim, long ldt, long n, const int32_t *__r
     for (long ch = h_lo / L + tid; ch <= (h_hi - 1) / L; ch += BX_THREADS) {
         const long a = ch * L, b = min(a + L, n);
         const double off = sc[ch];
+        const float oh = __double2float_rn(off), ol = __double2float_rn(__dsub_rn(off, (double)oh));
         float run = 0.f;
         for (long i = a; i < b; i++) {
             run = __fadd_rn(run, __fsub_rn(row[i], mean));
-            if (i >= h_lo && i < h_hi) c[i - h_lo] = __double2float_rn(__dadd_rn(off, (double)run));
+            if (i >= h_lo && i < h_hi) c[i - h_lo] = __fadd_rn(__fadd_rn(oh, run), ol);
         }
     }
     __syncthreads();
