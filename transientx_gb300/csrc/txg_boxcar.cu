@@ -360,10 +360,9 @@ k_boxcar(const float *__restrict__ tim, long ldt, long n, const int32_t *__restr
 /* The single-CTA kernel's arithmetic depends only on n: statistics by the fixed run pattern,
  * and the running sum over BX_THREADS chunks of L = ceil(n/BX_THREADS) samples (FP32 inside a
  * chunk, FP64 chunk offsets added as a float pair).  k_boxcar_prep computes, per row, the same
- * statistics and chunk
- * offsets from global memory; k_boxcar_seg rebuilds the running sum of a segment of chunks
- * plus a halo of the widest boxcar and runs the same width passes: results are identical to
- * k_boxcar's.  scratch row k: [0, BX_THREADS) chunk offsets, [BX_THREADS] mean and var. */
+ * statistics and chunk offsets from global memory; k_boxcar_seg rebuilds the running sum of a
+ * segment of chunks plus a halo of the widest boxcar and runs the same width passes: results
+ * are identical to k_boxcar's.  scratch row k: [0, BX_THREADS) chunk offsets, [BX_THREADS] mean and var. */
 constexpr int SEG_CHUNKS = 32; /* chunks per segment CTA */
 
 __global__ void __launch_bounds__(BX_THREADS)
