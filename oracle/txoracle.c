@@ -8,7 +8,7 @@
  * Conventions shared with the CUDA path (they make the two bit-comparable):
  *   - block data are channel-major, x[j*ldx + i], j = channel, i = time sample;
  *   - every float sum runs in the order written here, starting from 0.0f;
- *   - per-row reductions that need FP64 use txo_red32() (lane-strided FP32 runs of 8,
+ *   - per-row reductions that need FP64 use txo_red32() (lane-strided FP32 runs of 32,
  *     FP64 lane accumulators, 32-lane xor butterfly), which a warp computes identically.
  * See txoracle.h for the reference file:line each function follows.
  */
@@ -84,9 +84,10 @@ float txo_kadane(const float *y, long n, long *start, long *end)
 }
 
 /* Deterministic row reduction: mode 0 sums x, mode 1 sums x*x, mode 2 sums x*y (products
- * rounded to float).  Lane l (0..31) takes i = l, l+32, l+64, ... in runs of 8 summed in
- * FP32; each run total is added to the lane's FP64 accumulator; the 32 accumulators are
- * combined by an xor butterfly (offsets 16, 8, 4, 2, 1). */
+ * rounded to float).  Lane l (0..31) takes i = l, l+32, l+64, ... in runs of TXO_RED_RUN
+ * summed in FP32; each run total is added to the lane's FP64 accumulator; the 32
+ * accumulators are combined by an xor butterfly (offsets 16, 8, 4, 2, 1). */
+#define TXO_RED_RUN 32
 double txo_red32(const float *x, const float *y, long n, int mode)
 {
     double acc[32], tmp[32];
@@ -95,7 +96,7 @@ double txo_red32(const float *x, const float *y, long n, int mode)
         long i = l;
         while (i < n) {
             float run = 0.f;
-            for (int r = 0; r < 8 && i < n; r++, i += 32) {
+            for (int r = 0; r < TXO_RED_RUN && i < n; r++, i += 32) {
                 float v = mode == 0 ? x[i] : (mode == 1 ? x[i] * x[i] : x[i] * y[i]);
                 run = run + v;
             }

@@ -10,7 +10,7 @@
  * Every float operation uses an explicit round-to-nearest intrinsic so that no multiply-add
  * is fused: results are bit-identical to a scalar C evaluation of the same expressions in
  * the same order.  Row reductions that need FP64 follow one fixed pattern (lane-strided FP32
- * runs of 8, FP64 lane accumulators, xor butterfly), identical in every implementation.
+ * runs of 32, FP64 lane accumulators, xor butterfly), identical in every implementation.
  */
 #include <cstdio>
 
@@ -60,39 +60,6 @@ __device__ __forceinline__ void row_map(float *__restrict__ r, long n, int lane,
     for (long i = i0 + lane; i < n; i += 32) r[i] = f(r[i], i);
 }
 
-/* Fixed-pattern warp reduction of a row: mode 0 -> sum x, 1 -> sum x*x, 2 -> sum x*y. */
-template <int MODE>
-__device__ __forceinline__ double red32(const float *__restrict__ x, const float *__restrict__ y,
-                                        long n, int lane)
-{
-    double acc = 0.;
-    long i = lane;
-    for (; i + 7 * 32 < n; i += 8 * 32) { /* full runs: the eight loads first */
-        float v[8];
-#pragma unroll
-        for (int r = 0; r < 8; r++) {
-            v[r] = x[i + 32 * r];
-            if (MODE == 1) v[r] = __fmul_rn(v[r], v[r]);
-            if (MODE == 2) v[r] = __fmul_rn(v[r], y[i + 32 * r]);
-        }
-        float run = 0.f;
-#pragma unroll
-        for (int r = 0; r < 8; r++) run = __fadd_rn(run, v[r]);
-        acc = __dadd_rn(acc, (double)run);
-    }
-    if (i < n) { /* the last, partial run */
-        float run = 0.f;
-        for (; i < n; i += 32) {
-            float v = x[i];
-            if (MODE == 1) v = __fmul_rn(v, v);
-            if (MODE == 2) v = __fmul_rn(v, y[i]);
-            run = __fadd_rn(run, v);
-        }
-        acc = __dadd_rn(acc, (double)run);
-    }
-    return warp_sum_d(acc);
-}
-
 struct Ident {
     __device__ __forceinline__ float operator()(float v) const { return v; }
 };
@@ -103,26 +70,34 @@ struct Standardise {
     __device__ __forceinline__ float operator()(float v) const { return __fmul_rn(__fsub_rn(v, m), inv); }
 };
 
-/* Two fixed-pattern reductions of one row in a single pass (same per-lane order as red32):
- * MODE 1 -> (sum x, sum x*x), MODE 2 -> (sum x, sum x*y), x = f(stored value). */
+/* Two fixed-pattern reductions of one row by one warp: lane l takes i = l, l+32, l+64, ... in
+ * runs of RED_RUN summed in FP32, adds each run total to its FP64 accumulator, and the lanes
+ * combine by an xor butterfly.  MODE 1 -> (sum x, sum x*x), MODE 2 -> (sum x, sum x*y),
+ * x = f(stored value).  Long runs keep the FP64 work (a small share of this part's arithmetic
+ * rate) to two additions per 32 elements of a lane. */
+constexpr int RED_RUN = 32;
+
 template <int MODE, typename F = Ident>
 __device__ __forceinline__ void red32x2(const float *__restrict__ x, const float *__restrict__ y,
                                         long n, int lane, double &o1, double &o2, F f = F())
 {
     double a1 = 0., a2 = 0.;
     long i = lane;
-    for (; i + 7 * 32 < n; i += 8 * 32) { /* full runs: the eight loads first */
-        float v[8], q[8];
-#pragma unroll
-        for (int r = 0; r < 8; r++) {
-            v[r] = f(x[i + 32 * r]);
-            q[r] = MODE == 1 ? v[r] : y[i + 32 * r];
-        }
+    for (; i + (RED_RUN - 1) * 32 < n; i += RED_RUN * 32) { /* full runs, eight loads at a time */
         float r1 = 0.f, r2 = 0.f;
 #pragma unroll
-        for (int r = 0; r < 8; r++) {
-            r1 = __fadd_rn(r1, v[r]);
-            r2 = __fadd_rn(r2, __fmul_rn(v[r], q[r]));
+        for (int h = 0; h < RED_RUN / 8; h++) {
+            float v[8], q[8];
+#pragma unroll
+            for (int r = 0; r < 8; r++) {
+                v[r] = f(x[i + 32 * (8 * h + r)]);
+                q[r] = MODE == 1 ? v[r] : y[i + 32 * (8 * h + r)];
+            }
+#pragma unroll
+            for (int r = 0; r < 8; r++) {
+                r1 = __fadd_rn(r1, v[r]);
+                r2 = __fadd_rn(r2, __fmul_rn(v[r], q[r]));
+            }
         }
         a1 = __dadd_rn(a1, (double)r1);
         a2 = __dadd_rn(a2, (double)r2);
@@ -913,16 +888,16 @@ __global__ void __launch_bounds__(256) k_zdot_norm(const float *__restrict__ x, 
     }
 }
 
-/* se and ss of the zero-DM series in the fixed pattern of red32x2: lane l's runs of eight
- * elements (l + 32*(8*rho + r)) are summed in FP32 by all threads at once, then each lane
- * adds its run totals in FP64 in run order and the lanes combine by the xor butterfly. */
+/* se and ss of the zero-DM series in the fixed pattern of red32x2: lane l's runs of RED_RUN
+ * elements (l + 32*(RED_RUN*rho + r)) are summed in FP32 by all threads at once, then each
+ * lane adds its run totals in FP64 in run order and the lanes combine by the xor butterfly. */
 constexpr int SST_RUNS = 4096; /* run totals staged per lane set (2 floats each) */
 
 __global__ void __launch_bounds__(1024) k_zdot_sstats(const float *__restrict__ s, long N,
                                                      double *__restrict__ out)
 {
     __shared__ float run1[SST_RUNS], run2[SST_RUNS];
-    const long nruns = ((N + 31) / 32 + 7) / 8; /* runs of the longest lane */
+    const long nruns = ((N + 31) / 32 + RED_RUN - 1) / RED_RUN; /* runs of the longest lane */
     double a1 = 0., a2 = 0.;
     for (long base = 0; base < nruns; base += SST_RUNS / 32) {
         const long nb = min((long)(SST_RUNS / 32), nruns - base);
@@ -930,8 +905,8 @@ __global__ void __launch_bounds__(1024) k_zdot_sstats(const float *__restrict__ 
             const long rho = base + u / 32, l = u % 32;
             float r1 = 0.f, r2 = 0.f;
 #pragma unroll
-            for (int r = 0; r < 8; r++) {
-                const long i = l + 32 * (8 * rho + r);
+            for (int r = 0; r < RED_RUN; r++) {
+                const long i = l + 32 * (RED_RUN * rho + r);
                 if (i < N) {
                     const float v = s[i];
                     r1 = __fadd_rn(r1, v);
