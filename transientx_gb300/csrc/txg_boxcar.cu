@@ -29,6 +29,7 @@ constexpr int BX_U = 4;  /* samples per thread per pass, tracked search: width p
 constexpr int BX_UF = 8; /* the same for the maximum-only search */
 constexpr unsigned FULL = 0xffffffffu;
 constexpr size_t BX_SMEM_MAX = 200 * 1024; /* + ~10 KB static stays under 227 KB */
+constexpr int BX_RUN = 32; /* row statistics: FP32 runs per thread before each FP64 addition */
 
 __device__ __forceinline__ double block_sum_d(double v, double *red)
 {
@@ -260,7 +261,7 @@ k_boxcar(const float *__restrict__ tim, long ldt, long n, const int32_t *__restr
         long i = tid;
         while (i < n) {
             float r1 = 0.f, r2 = 0.f;
-            for (int r = 0; r < 8 && i < n; r++, i += BX_THREADS) {
+            for (int r = 0; r < BX_RUN && i < n; r++, i += BX_THREADS) {
                 float v = c[i];
                 r1 = __fadd_rn(r1, v);
                 r2 = __fadd_rn(r2, __fmul_rn(v, v));
@@ -380,7 +381,7 @@ k_boxcar_prep(const float *__restrict__ tim, long ldt, long n, int iqr, double *
         long i = tid;
         while (i < n) {
             float r1 = 0.f, r2 = 0.f;
-            for (int r = 0; r < 8 && i < n; r++, i += BX_THREADS) {
+            for (int r = 0; r < BX_RUN && i < n; r++, i += BX_THREADS) {
                 float v = row[i];
                 r1 = __fadd_rn(r1, v);
                 r2 = __fadd_rn(r2, __fmul_rn(v, v));
