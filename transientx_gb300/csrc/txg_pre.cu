@@ -38,8 +38,9 @@ __device__ __forceinline__ long long warp_sum_ll(long long v)
     return v;
 }
 
-/* r[i] = f(r[i], i) over a row by one warp, 16-byte accesses when the row is aligned (each
- * element is independent, so the access width does not change any result). */
+/* r[i] = f(r[i], i) over a row by one warp, 16-byte accesses when the row is aligned, four
+ * of them in flight per lane (each element is independent, so the access width does not
+ * change any result). */
 template <typename F>
 __device__ __forceinline__ void row_map(float *__restrict__ r, long n, int lane, F f)
 {
@@ -47,7 +48,22 @@ __device__ __forceinline__ void row_map(float *__restrict__ r, long n, int lane,
     if ((reinterpret_cast<uintptr_t>(r) & 15) == 0) {
         const long n4 = n / 4;
         float4 *r4 = reinterpret_cast<float4 *>(r);
-        for (long q = lane; q < n4; q += 32) {
+        long q = lane;
+        for (; q + 3 * 32 < n4; q += 4 * 32) {
+            float4 v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) v[u] = r4[q + 32 * u];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const long b = 4 * (q + 32 * u);
+                v[u].x = f(v[u].x, b);
+                v[u].y = f(v[u].y, b + 1);
+                v[u].z = f(v[u].z, b + 2);
+                v[u].w = f(v[u].w, b + 3);
+                r4[q + 32 * u] = v[u];
+            }
+        }
+        for (; q < n4; q += 32) {
             float4 v = r4[q];
             v.x = f(v.x, 4 * q);
             v.y = f(v.y, 4 * q + 1);
