@@ -220,6 +220,7 @@ struct BeamPrep {
 using namespace txg;
 
 struct txg_handle {
+    int device = 0; /* the CUDA device current at txg_create */
     txg_plan plan;
     std::vector<double> freqs;
     std::vector<txg_row> rows;
@@ -241,6 +242,26 @@ struct txg_handle {
     double class_ms[NCLASS] = {0};
     long class_n[NCLASS] = {0};
     std::vector<void *> allocs;
+};
+
+/* Makes the handle's device current for the duration of an entry point and restores the
+ * caller's current device on return, so that handles on different devices can be driven from
+ * one thread. */
+struct DeviceScope {
+    int prev = -1;
+    explicit DeviceScope(const txg_handle *h)
+    {
+        int cur = -1;
+        if (h && cudaGetDevice(&cur) == cudaSuccess && cur != h->device &&
+            cudaSetDevice(h->device) == cudaSuccess)
+            prev = cur;
+    }
+    ~DeviceScope()
+    {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+    DeviceScope(const DeviceScope &) = delete;
+    DeviceScope &operator=(const DeviceScope &) = delete;
 };
 
 namespace {
@@ -676,6 +697,7 @@ int txg_create(const txg_plan *plan, txg_handle **out)
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1)
         return fail(TXG_ERR_NODEVICE, "no CUDA device");
     txg_handle *h = new txg_handle();
+    if (cudaGetDevice(&h->device) != cudaSuccess) h->device = 0;
     h->plan = *plan;
     h->freqs.assign(plan->frequencies, plan->frequencies + plan->nchans);
     h->rows.assign(plan->rows, plan->rows + plan->nrows);
@@ -816,6 +838,7 @@ int txg_create(const txg_plan *plan, txg_handle **out)
 
 void txg_destroy(txg_handle *h)
 {
+    DeviceScope device_scope(h);
     if (!h) return;
     free_all(h);
     delete h;
@@ -823,6 +846,7 @@ void txg_destroy(txg_handle *h)
 
 int txg_push_block_device(txg_handle *h, int32_t beam, const uint8_t *dev, int64_t nsamp)
 {
+    DeviceScope device_scope(h);
     if (!h || !dev) return fail(TXG_ERR_ARG, "null handle or buffer");
     if (beam < 0 || beam >= (int)h->br.size()) return fail(TXG_ERR_ARG, "beam out of range");
     if (nsamp != h->plan.ndump) return fail(TXG_ERR_ARG, "nsamp must equal the plan's ndump");
@@ -831,6 +855,7 @@ int txg_push_block_device(txg_handle *h, int32_t beam, const uint8_t *dev, int64
 
 int txg_push_block(txg_handle *h, int32_t beam, const uint8_t *host, int64_t nsamp)
 {
+    DeviceScope device_scope(h);
     if (!h || !host) return fail(TXG_ERR_ARG, "null handle or buffer");
     if (beam < 0 || beam >= (int)h->br.size()) return fail(TXG_ERR_ARG, "beam out of range");
     if (nsamp != h->plan.ndump) return fail(TXG_ERR_ARG, "nsamp must equal the plan's ndump");
@@ -860,6 +885,7 @@ int txg_push_block(txg_handle *h, int32_t beam, const uint8_t *host, int64_t nsa
 
 int txg_sync(txg_handle *h)
 {
+    DeviceScope device_scope(h);
     if (!h) return fail(TXG_ERR_ARG, "null handle");
     TXG_CUDA_TRY(cudaStreamSynchronize(h->st));
     int status = TXG_OK;
@@ -891,6 +917,7 @@ int txg_get_row_info(txg_handle *h, int32_t beam, int32_t row, txg_row_info *out
 
 int txg_get_candidates(txg_handle *h, int32_t beam, int32_t row, txg_cand *out, int64_t cap, int64_t *n)
 {
+    DeviceScope device_scope(h);
     int rc = check_beam_row(h, beam, row);
     if (rc) return rc;
     const BeamRow &b = h->br[beam][row];
@@ -907,6 +934,7 @@ int txg_get_candidates(txg_handle *h, int32_t beam, int32_t row, txg_cand *out, 
 int txg_pop_result(txg_handle *h, int32_t beam, int32_t row, txg_result *res, txg_cand *points,
                    int64_t pcap, txg_cand *clusters, int64_t ccap)
 {
+    DeviceScope device_scope(h);
     int rc = check_beam_row(h, beam, row);
     if (rc) return rc;
     BeamRow &b = h->br[beam][row];
@@ -948,6 +976,7 @@ int txg_result_ready(txg_handle *h, int32_t beam, int32_t row, int32_t *ready)
 
 int txg_get_dense(txg_handle *h, int32_t beam, int32_t row, float *mxS, int32_t *mxwn)
 {
+    DeviceScope device_scope(h);
     int rc = check_beam_row(h, beam, row);
     if (rc) return rc;
     if (!(h->flags & TXG_FLAG_DENSE)) return fail(TXG_ERR_STATE, "plan was created without TXG_FLAG_DENSE");
@@ -962,6 +991,7 @@ int txg_get_dense(txg_handle *h, int32_t beam, int32_t row, float *mxS, int32_t 
 
 int txg_get_timdata(txg_handle *h, int32_t beam, int32_t row, int64_t idm0, int64_t count, float *out)
 {
+    DeviceScope device_scope(h);
     int rc = check_beam_row(h, beam, row);
     if (rc) return rc;
     const RowPlan &P = h->rp[row];
@@ -1023,6 +1053,7 @@ __global__ void k_tim_quant(const float *__restrict__ tim, long ldt, long nsamp,
 int txg_get_timdata_q(txg_handle *h, int32_t beam, int32_t row, int64_t idm0, int64_t count,
                       int64_t nsamp, int32_t nbits, float mean, float std, void *out)
 {
+    DeviceScope device_scope(h);
     int rc = check_beam_row(h, beam, row);
     if (rc) return rc;
     const RowPlan &P = h->rp[row];
@@ -1045,6 +1076,7 @@ int txg_get_timdata_q(txg_handle *h, int32_t beam, int32_t row, int64_t idm0, in
 
 int txg_get_block(txg_handle *h, int32_t beam, int32_t row, float *out)
 {
+    DeviceScope device_scope(h);
     int rc = check_beam_row(h, beam, row);
     if (rc) return rc;
     if (!out) return fail(TXG_ERR_ARG, "null output");
@@ -1060,6 +1092,7 @@ int txg_get_block(txg_handle *h, int32_t beam, int32_t row, float *out)
 
 int txg_get_zap_ranges(txg_handle *h, int32_t beam, int32_t row, int32_t irfi, int32_t *out, int64_t cap)
 {
+    DeviceScope device_scope(h);
     int rc = check_beam_row(h, beam, row);
     if (rc) return rc;
     const RowPlan &P = h->rp[row];
@@ -1100,6 +1133,7 @@ static int last_block_window(txg_handle *h, int32_t beam, int32_t row, long *t0_
 
 int txg_get_subdata(txg_handle *h, int32_t beam, int32_t row, int64_t idm, float *out)
 {
+    DeviceScope device_scope(h);
     long t0_mod = 0;
     int rc = last_block_window(h, beam, row, &t0_mod);
     if (rc) return rc;
@@ -1121,6 +1155,7 @@ int txg_get_subdata(txg_handle *h, int32_t beam, int32_t row, int64_t idm, float
 int txg_cand_band(txg_handle *h, int32_t beam, int32_t row, const txg_cand *c, int64_t n,
                   float *fl, float *fh)
 {
+    DeviceScope device_scope(h);
     long t0_mod = 0;
     int rc = last_block_window(h, beam, row, &t0_mod);
     if (rc) return rc;
@@ -1174,6 +1209,7 @@ int txg_cand_band(txg_handle *h, int32_t beam, int32_t row, const txg_cand *c, i
 
 int txg_get_mask(txg_handle *h, int32_t beam, uint8_t *mask)
 {
+    DeviceScope device_scope(h);
     if (!h || !mask) return fail(TXG_ERR_ARG, "null argument");
     if (beam < 0 || beam >= (int)h->prep.size()) return fail(TXG_ERR_ARG, "beam out of range");
     TXG_CUDA_TRY(cudaStreamSynchronize(h->st));
@@ -1183,6 +1219,7 @@ int txg_get_mask(txg_handle *h, int32_t beam, uint8_t *mask)
 
 int txg_get_tables(txg_handle *h, int32_t row, int32_t *d1, int32_t *d2, int32_t *sub_start, int32_t *vwn)
 {
+    DeviceScope device_scope(h);
     if (!h || row < 0 || row >= (int)h->rp.size()) return fail(TXG_ERR_ARG, "row out of range");
     copy_tables(h->rp[row], d1, d2, sub_start, vwn);
     return TXG_OK;
@@ -1205,6 +1242,7 @@ int txg_describe_row(const txg_plan *plan, int32_t row, txg_row_info *info, int3
 
 int txg_get_timing(txg_handle *h, double *ms, int64_t *launches, int32_t n)
 {
+    DeviceScope device_scope(h);
     if (!h) return fail(TXG_ERR_ARG, "null handle");
     for (int c = 0; c < NCLASS && c < n; c++) {
         if (ms) ms[c] = h->class_ms[c];

@@ -1013,11 +1013,10 @@ bool launch_unpack(const uint8_t *raw, int C_raw, long n0, int td, int fd, float
     }
     size_t smem = (size_t)UP_TI * td * UP_TJ * fd;
     if (smem <= 96 * 1024) {
-        static bool attr = false;
-        if (!attr) {
+        /* per call: the attribute belongs to the current device, and handles may live on
+         * different devices of one process */
+        if (smem > 48 * 1024)
             cudaFuncSetAttribute(k_unpack, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
-            attr = true;
-        }
         dim3 grid(nblk(N, UP_TI), nblk(C, UP_TJ));
         k_unpack<<<grid, 256, smem, st>>>(raw, C_raw, n0, td, fd, x, ldx, C, N, mask);
     } else {
