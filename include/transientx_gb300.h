@@ -225,6 +225,14 @@ int txg_describe_row(const txg_plan *plan, int32_t row, txg_row_info *info, int3
                      int32_t *d2, int32_t *sub_start, int32_t *vwn);
 
 /* Boxcar width ladder of SinglePulse::prepare (singlepulse.cpp:242-254); returns the count. */
+/* Self-test of the failure path of every kernel that waits for its shared-memory copies: one
+ * CTA waits, with the same bounded wait, for a 256-byte bulk copy.  never_complete = 0: the copy
+ * completes (TXG_OK).  never_complete != 0: its barrier expects more bytes than the copy brings,
+ * the wait runs out after limit_ms (1..10000) of GPU clock and the kernel reports it:
+ * TXG_ERR_TIMEOUT, the CUDA context stays usable.  (The kernels' own waits give up after 2 s.)
+ * No reference counterpart. */
+int txg_selftest_wait(int32_t never_complete, int32_t limit_ms);
+
 int txg_width_ladder(float minw, float maxw, float snrloss, double tsamp, int32_t *vwn,
                      int32_t cap);
 

@@ -237,6 +237,22 @@ def test_reduced_precision_series(tx, prec, bound):
             assert err.max() < bound, (prec, r, err.max())
 
 
+def test_bounded_wait_gives_up_and_context_stays_usable(tx):
+    """A barrier that never completes: the kernel's bounded wait runs out after the limit and
+    reports TXG_ERR_TIMEOUT; the context keeps working (a completing copy, then a search)."""
+    import time
+    assert tx.selftest_wait(False, 500) == tx.OK
+    t0 = time.perf_counter()
+    assert tx.selftest_wait(True, 200) == tx.ERR_TIMEOUT
+    assert 0.15 < time.perf_counter() - t0 < 10.0
+    assert tx.selftest_wait(False, 500) == tx.OK
+    fil, rows, ndump = small_workload()
+    with tx.Search(rows, fil.nchans, fil.tsamp, fil.freqs, ndump) as s:
+        for b in range(2):
+            s.push_block(fil.generate(b * ndump, ndump))
+        s.sync()
+
+
 def test_result_ready_polls_without_waiting(tx):
     """txg_result_ready: None with nothing waiting; after sync every waiting block is ready and
     pops in push order with the same results as a blocking pop."""

@@ -106,6 +106,7 @@ EXPORTS = [
     "txg_cluster", "txg_get_timing", "txg_get_stream", "txg_strerror", "txg_version",
     "txg_describe_row", "txg_pop_result", "txg_get_mask", "txg_kadaneF_noalloc",
     "txg_get_subdata", "txg_cand_band", "txg_replot", "txg_get_timdata_q", "txg_result_ready",
+    "txg_selftest_wait",
 ]
 
 _lib: Optional[C.CDLL] = None
@@ -158,6 +159,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.txg_pop_result.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(txg_result), vp, C.c_int64,
                                  vp, C.c_int64]
     L.txg_result_ready.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(C.c_int32)]
+    L.txg_selftest_wait.argtypes = [C.c_int32, C.c_int32]
     L.txg_describe_row.argtypes = [C.POINTER(txg_plan), C.c_int32, C.POINTER(txg_row_info), vp,
                                    vp, vp, vp]
     _lib = L
@@ -524,6 +526,12 @@ class Search:
             cands = self.candidates(row, beam)
         return cluster(cands, i.dms, i.ddm, i.fmax, i.fmin, i.tsamp, sp.radius_smearing,
                        sp.maxncand, sp.minpts, sp.remove_cand_with_maxwidth, i.maxwn)
+
+
+def selftest_wait(never_complete: bool, limit_ms: int = 200) -> int:
+    """The bounded device wait of the shared-memory copies, on a copy that completes or on a
+    barrier that never completes (then TXG_ERR_TIMEOUT after limit_ms); returns the status."""
+    return int(load_library().txg_selftest_wait(1 if never_complete else 0, int(limit_ms)))
 
 
 def boxcar(tim: np.ndarray, vwn: Sequence[int], iqr: bool = False, avx2_tail: bool = False,

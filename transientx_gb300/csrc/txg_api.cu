@@ -678,6 +678,35 @@ const char *txg_strerror(int32_t status)
     return s.c_str();
 }
 
+int txg_selftest_wait(int32_t never_complete, int32_t limit_ms)
+{
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return fail(TXG_ERR_NODEVICE, "no CUDA device");
+    if (limit_ms < 1 || limit_ms > 10000) return fail(TXG_ERR_ARG, "limit_ms must lie in [1, 10000]");
+    uint8_t *src = nullptr;
+    int *dstatus = nullptr;
+    cudaStream_t st = nullptr;
+    int hstatus = -1;
+    cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&src, 256);
+    if (e == cudaSuccess) e = cudaMalloc(&dstatus, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemsetAsync(src, 0x5a, 256, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(dstatus, 0xff, sizeof(int), st);
+    if (e == cudaSuccess) {
+        launch_wait_selftest(src, never_complete ? 256 : 0, limit_ms, dstatus, st);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hstatus, dstatus, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (src) cudaFree(src);
+    if (dstatus) cudaFree(dstatus);
+    if (st) cudaStreamDestroy(st);
+    if (e != cudaSuccess) return set_cuda_error(e, "txg_selftest_wait", __FILE__, __LINE__);
+    if (hstatus == 1) return fail(TXG_ERR_TIMEOUT, "a bounded device wait gave up (self-test)");
+    if (hstatus != 0) return fail(TXG_ERR_CUDA, "self-test copy arrived wrong");
+    return TXG_OK;
+}
+
 int txg_width_ladder(float minw, float maxw, float snrloss, double tsamp, int32_t *vwn, int32_t cap)
 {
     if (!vwn || cap <= 0) return 0;

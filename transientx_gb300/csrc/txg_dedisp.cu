@@ -82,17 +82,32 @@ __device__ __forceinline__ void cp_async4(void *dst, const void *src)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
-/* Bounded wait on phase `parity`; returns false if it gave up. */
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+/* Nanosecond clock of the GPU. */
+__device__ __forceinline__ uint64_t gtimer()
 {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+/* A window copy lands in microseconds; a wait that has not seen its phase complete after this
+ * long gives up (the kernel then reports an error instead of hanging). */
+constexpr uint64_t MBAR_LIMIT_NS = 2000000000ull;
+
+/* Bounded wait on phase `parity`: gives up (returns false) after limit_ns of the GPU clock,
+ * or after 2^30 polls should that clock not advance. */
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint64_t limit_ns = MBAR_LIMIT_NS)
+{
+    const uint64_t t0 = gtimer();
     uint32_t done = 0;
-    for (long it = 0; it < (1L << 24); it++) {
+    for (long it = 0; it < (1L << 30); it++) {
         asm volatile(
             "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
             : "=r"(done)
             : "r"(smem_addr(bar)), "r"(parity)
             : "memory");
         if (done) return true;
+        if (gtimer() - t0 > limit_ns) return false;
     }
     return false;
 }
@@ -1105,6 +1120,36 @@ static void stage2_dispatch(int var, const void *ring, long R, int nsub, int G, 
     default: TXG_S2(32); break;
     }
 #undef TXG_S2
+}
+
+/* One CTA waits, with the bounded wait of the window copies, for a 256-byte bulk copy whose
+ * barrier expects 256 + extra bytes: with extra > 0 the phase never completes (the copy lands,
+ * nothing else comes), the wait runs out after limit_ns and the CTA reports it in status[0]. */
+__global__ void k_wait_selftest(const uint8_t *__restrict__ src, int extra, uint64_t limit_ns,
+                                int *__restrict__ status)
+{
+    __shared__ __align__(16) unsigned char buf[256];
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_expect_tx(&bar, 256u + (uint32_t)extra);
+        bulk_g2s(buf, src, 256u, &bar);
+    }
+    const bool ok = mbar_wait(&bar, 0, limit_ns);
+    if (!__syncthreads_and(ok)) {
+        if (threadIdx.x == 0) status[0] = 1;
+        return;
+    }
+    if (threadIdx.x == 0) status[0] = buf[0] == src[0] && buf[255] == src[255] ? 0 : 2;
+}
+
+void launch_wait_selftest(const uint8_t *src, int extra, long limit_ms, int *status, cudaStream_t st)
+{
+    k_wait_selftest<<<1, 32, 0, st>>>(src, extra, (uint64_t)limit_ms * 1000000ull, status);
 }
 
 void launch_stage2(const void *ring, long R, int nsub, int G, long ndm, long nout,

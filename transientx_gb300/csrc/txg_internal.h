@@ -119,6 +119,9 @@ long stage2_window(long span);
 void launch_stage2(const void *ring, long R, int nsub, int G, long ndm, long nout,
                    const int32_t *d2, long span, long t0_mod, int prec, int s2_var, int s2_kb,
                    float *tim, long ldt, int *err, cudaStream_t st);
+/* the bounded wait of the window copies on a copy that completes (extra = 0) or on a barrier
+ * expecting extra bytes more than arrive; status[0]: 0 completed, 1 gave up */
+void launch_wait_selftest(const uint8_t *src, int extra, long limit_ms, int *status, cudaStream_t st);
 /* the subband series of fine DM k ([nsub][nout] floats) and, per candidate, the per-subband
  * sums over its window (vpf [n][nsub]) from the subband ring */
 void launch_subdata(const void *ring, long R, int nsub, int G, const int32_t *d2, long k,
