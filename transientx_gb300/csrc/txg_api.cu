@@ -231,6 +231,13 @@ struct txg_handle {
     cudaStream_t st = nullptr;
     cudaStream_t cst = nullptr; /* host-to-device copies of raw blocks */
     cudaStream_t dst = nullptr; /* device-to-host copies of candidates */
+    /* one stream per ddplan row: the rows of a block run concurrently (the single-CTA and
+     * latency-bound kernels and the last waves of one row leave SMs to the others); each
+     * forks from the handle stream after the block's shared steps (raw copy, channel zap)
+     * and joins it at the end of the block */
+    std::vector<cudaStream_t> rst;
+    std::vector<cudaEvent_t> row_done;
+    cudaEvent_t fork = nullptr;
     uint8_t *raw[2] = {nullptr, nullptr};
     uint8_t *stage[2] = {nullptr, nullptr}; /* pinned staging for pageable host input */
     cudaEvent_t raw_free[2] = {nullptr, nullptr};   /* kernels done with raw[i] */
@@ -307,6 +314,8 @@ size_t ring_elem(int prec) { return prec == TXG_PREC_FP32 ? 4 : 2; }
 
 void free_all(txg_handle *h)
 {
+    for (cudaStream_t s : h->rst)
+        if (s) cudaStreamSynchronize(s);
     if (h->st) cudaStreamSynchronize(h->st);
     if (h->cst) cudaStreamSynchronize(h->cst);
     if (h->dst) cudaStreamSynchronize(h->dst);
@@ -329,6 +338,14 @@ void free_all(txg_handle *h)
         if (h->raw_free[i]) cudaEventDestroy(h->raw_free[i]);
         if (h->raw_loaded[i]) cudaEventDestroy(h->raw_loaded[i]);
     }
+    for (cudaStream_t s : h->rst)
+        if (s) cudaStreamDestroy(s);
+    for (cudaEvent_t e : h->row_done)
+        if (e) cudaEventDestroy(e);
+    h->rst.clear();
+    h->row_done.clear();
+    if (h->fork) cudaEventDestroy(h->fork);
+    h->fork = nullptr;
     if (h->st) cudaStreamDestroy(h->st);
     if (h->cst) cudaStreamDestroy(h->cst);
     if (h->dst) cudaStreamDestroy(h->dst);
@@ -484,15 +501,20 @@ int run_block(txg_handle *h, int beam, const uint8_t *raw)
         TXG_CUDA_TRY(cudaGetLastError());
         mask = bp.mask;
     }
+    TXG_CUDA_TRY(cudaEventRecord(h->fork, h->st));
     for (size_t r = 0; r < h->rp.size(); r++) {
         const RowPlan &P = h->rp[r];
         RowDev &D = h->rd[r];
         BeamRow &b = h->br[beam][r];
         Slot &sl = b.slot[b.nblocks % NSLOT];
+        /* with per-kernel-class timing the rows run one after another on the handle stream,
+         * so that each class's event span holds its own kernels only */
+        const cudaStream_t rs = timing ? h->st : h->rst[r];
         int rc = harvest(h, b, sl, P);
         if (rc && rc != TXG_ERR_OVERFLOW) return rc;
         if (rc) status = rc;
-        if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[0], h->st));
+        TXG_CUDA_TRY(cudaStreamWaitEvent(rs, h->fork, 0));
+        if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[0], rs));
 
         /* history: the last H columns of the previous block go in front of this one */
         /* one buffer when the history is shorter than a block (the previous block's last H
@@ -501,69 +523,69 @@ int run_block(txg_handle *h, int beam, const uint8_t *raw)
         if (P.H > 0)
             TXG_CUDA_TRY(cudaMemcpy2DAsync(xcur, P.ldh * sizeof(float), xprev + P.N,
                                            P.ldh * sizeof(float), P.H * sizeof(float), P.C,
-                                           cudaMemcpyDeviceToDevice, h->st));
+                                           cudaMemcpyDeviceToDevice, rs));
         float *x = xcur + P.H;
         const bool part = launch_unpack(raw, Craw, n0, P.cfg.td, P.cfg.fd, x, P.ldh, P.C, P.N, mask,
-                                        b.eqpart, h->st);
-        if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[1], h->st));
+                                        b.eqpart, rs);
+        if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[1], rs));
 
         /* equalize from the unpack's integer sums; its apply rides on the baseline pass */
-        launch_eq_params(part ? b.eqpart : nullptr, x, P.ldh, P.C, P.N, b.eqp, b.live, h->st);
+        launch_eq_params(part ? b.eqpart : nullptr, x, P.ldh, P.C, P.N, b.eqp, b.live, rs);
         if (P.bl_nw > 0) {
-            launch_colmean(x, P.ldh, P.C, P.N, b.live, b.eqp, b.z, h->st);
-            launch_smooth(b.z, P.N, P.bl_nw, b.b, h->st);
-            launch_eq_apply(x, P.ldh, P.C, P.N, b.eqp, b.b, b.live, h->st);
+            launch_colmean(x, P.ldh, P.C, P.N, b.live, b.eqp, b.z, rs);
+            launch_smooth(b.z, P.N, P.bl_nw, b.b, rs);
+            launch_eq_apply(x, P.ldh, P.C, P.N, b.eqp, b.b, b.live, rs);
         } else {
-            launch_eq_apply(x, P.ldh, P.C, P.N, b.eqp, nullptr, b.live, h->st);
+            launch_eq_apply(x, P.ldh, P.C, P.N, b.eqp, nullptr, b.live, rs);
         }
         if (!P.zap_chan.empty())
-            launch_zero_rows(x, P.ldh, D.zap, (int)P.zap_chan.size(), P.N, h->st);
+            launch_zero_rows(x, P.ldh, D.zap, (int)P.zap_chan.size(), P.N, rs);
         for (int q = 0; q < P.cfg.nrfi; q++) {
             if (P.cfg.rfi_kind[q] == TXG_RFI_KADANEF)
                 launch_kadane(x, P.ldh, P.C, P.N, P.cfg.rfi_td[q], P.cfg.rfi_fd[q], P.kad_thr,
-                              P.kad_wnlimit[q], b.ds, b.ranges[q], h->st);
+                              P.kad_wnlimit[q], b.ds, b.ranges[q], rs);
             else if (P.cfg.rfi_kind[q] == TXG_RFI_ZDOT)
-                launch_zdot(x, P.ldh, P.C, P.N, b.s, b.sst, b.zp, h->st);
+                launch_zdot(x, P.ldh, P.C, P.N, b.s, b.sst, b.zp, rs);
             else if (P.cfg.rfi_kind[q] == TXG_RFI_KADANET)
                 launch_kadaneT(x, P.ldh, P.C, P.N, P.cfg.rfi_td[q], P.cfg.rfi_fd[q], P.kadT_thr,
-                               P.kad_wnlimit[q], b.ds, b.ranges[q], h->st);
+                               P.kad_wnlimit[q], b.ds, b.ranges[q], rs);
             else if (P.cfg.rfi_kind[q] == TXG_RFI_MASK)
                 launch_mask(x, P.ldh, P.C, P.N, P.cfg.rfi_td[q], P.cfg.rfi_fd[q], P.mask_thr, b.ds,
-                            b.sel, b.ranges[q], h->st);
+                            b.sel, b.ranges[q], rs);
             else if (P.cfg.rfi_kind[q] == TXG_RFI_ZERO) {
                 /* zero-DM filter: the live-channel mean series off every live channel */
-                launch_colmean(x, P.ldh, P.C, P.N, b.live, nullptr, b.z, h->st);
-                launch_sub_series(x, P.ldh, P.C, P.N, b.z, b.live, h->st);
+                launch_colmean(x, P.ldh, P.C, P.N, b.live, nullptr, b.z, rs);
+                launch_sub_series(x, P.ldh, P.C, P.N, b.z, b.live, rs);
             }
         }
         /* 16-bit precisions: stage 1 reads an FP16 copy (history columns included) */
-        if (b.x16) launch_to_half(xcur, P.ldh, P.C, P.H + P.N, b.x16, h->st);
-        if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[2], h->st));
+        if (b.x16) launch_to_half(xcur, P.ldh, P.C, P.H + P.N, b.x16, rs);
+        if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[2], rs));
 
         /* stage 1: new subband samples t in [counter-N-maxd1, counter-maxd1) */
         const long counter = b.pushed + P.N;
         const long tbase = counter - P.N - P.maxd1;
-        TXG_CUDA_TRY(cudaMemsetAsync(sl.dcount, 0, 2 * sizeof(int), h->st));
+        TXG_CUDA_TRY(cudaMemsetAsync(sl.dcount, 0, 2 * sizeof(int), rs));
         launch_stage1(xcur, b.x16, P.ldh, P.H - P.maxd1, P.C, P.N, P.nsub, P.ng, D.sub_start, D.d1,
                       P.maxd1, P.maxch, b.ring, P.R, pmod(tbase, P.R), h->prec, P.s1_var,
-                      sl.dcount + 1, h->st);
+                      sl.dcount + 1, rs);
         TXG_CUDA_TRY(cudaGetLastError());
-        if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[3], h->st));
+        if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[3], rs));
 
         const bool gated = counter >= P.offset - P.noverlap + P.N;
         if (gated) {
             const long t0 = counter - P.N - P.offset;
             launch_stage2(b.ring, P.R, P.nsub, P.G, P.cfg.ndm, P.nout, D.d2, P.s2_span,
-                          pmod(t0, P.R), h->prec, P.s2_var, P.s2_kb, b.tim, P.nout, sl.dcount + 1, h->st);
+                          pmod(t0, P.R), h->prec, P.s2_var, P.s2_kb, b.tim, P.nout, sl.dcount + 1, rs);
             TXG_CUDA_TRY(cudaGetLastError());
-            if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[4], h->st));
+            if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[4], rs));
             rc = launch_boxcar(b.tim, P.nout, P.cfg.ndm, P.nout, D.vwn, (int)P.vwn.size(), P.maxwn,
                                P.cfg.iqr, (h->flags & TXG_FLAG_AVX2_TAIL) ? 1 : 0, P.cfg.thre,
                                sl.dcand, sl.dcount, h->cap, b.mxS, b.mxwn, b.bx_scratch,
-                               sl.dcount + 1, h->st);
+                               sl.dcount + 1, rs);
             if (rc) return rc;
             TXG_CUDA_TRY(cudaGetLastError());
-            if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[5], h->st));
+            if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[5], rs));
             /* read-back on the copy stream, overlapping the next kernels: the row's expected
              * count of candidates (the rest, if any, is fetched at harvest) and the count.
              * The buffer's previous reader (two uses of this slot ago) must be done. */
@@ -573,7 +595,7 @@ int run_block(txg_handle *h, int beam, const uint8_t *raw)
                 sl.reader[sl.buf].reset();
             }
             sl.nread = std::min(b.guess, h->hcap);
-            TXG_CUDA_TRY(cudaEventRecord(sl.boxed, h->st));
+            TXG_CUDA_TRY(cudaEventRecord(sl.boxed, rs));
             TXG_CUDA_TRY(cudaStreamWaitEvent(h->dst, sl.boxed, 0));
             TXG_CUDA_TRY(cudaMemcpyAsync(sl.hbuf[sl.buf], sl.dcand, sl.nread * sizeof(txg_cand),
                                          cudaMemcpyDeviceToHost, h->dst));
@@ -581,11 +603,11 @@ int run_block(txg_handle *h, int beam, const uint8_t *raw)
             TXG_CUDA_TRY(cudaEventRecord(sl.done, h->dst));
         } else {
             if (timing) {
-                TXG_CUDA_TRY(cudaEventRecord(sl.ev[4], h->st));
-                TXG_CUDA_TRY(cudaEventRecord(sl.ev[5], h->st));
+                TXG_CUDA_TRY(cudaEventRecord(sl.ev[4], rs));
+                TXG_CUDA_TRY(cudaEventRecord(sl.ev[5], rs));
             }
-            TXG_CUDA_TRY(cudaMemcpyAsync(sl.hcount, sl.dcount, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
-            TXG_CUDA_TRY(cudaEventRecord(sl.done, h->st));
+            TXG_CUDA_TRY(cudaMemcpyAsync(sl.hcount, sl.dcount, 2 * sizeof(int), cudaMemcpyDeviceToHost, rs));
+            TXG_CUDA_TRY(cudaEventRecord(sl.done, rs));
         }
         sl.pending = true;
         sl.gated = gated;
@@ -593,6 +615,8 @@ int run_block(txg_handle *h, int beam, const uint8_t *raw)
         b.pushed = counter;
         b.nblocks++;
         if (b.xh[1]) b.cur ^= 1;
+        TXG_CUDA_TRY(cudaEventRecord(h->row_done[r], rs));
+        TXG_CUDA_TRY(cudaStreamWaitEvent(h->st, h->row_done[r], 0));
     }
     return status;
 }
@@ -786,6 +810,14 @@ int txg_create(const txg_plan *plan, txg_handle **out)
             cudaEventCreateWithFlags(&h->raw_loaded[i], cudaEventDisableTiming) != cudaSuccess)
             return bail(fail(TXG_ERR_CUDA, "event creation failed"));
     }
+    h->rst.assign(plan->nrows, nullptr);
+    h->row_done.assign(plan->nrows, nullptr);
+    if (cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming) != cudaSuccess)
+        return bail(fail(TXG_ERR_CUDA, "event creation failed"));
+    for (int r = 0; r < plan->nrows; r++)
+        if (cudaStreamCreateWithFlags(&h->rst[r], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&h->row_done[r], cudaEventDisableTiming) != cudaSuccess)
+            return bail(fail(TXG_ERR_CUDA, "row stream creation failed"));
     h->rd.resize(plan->nrows);
     for (int r = 0; r < plan->nrows; r++) {
         RowPlan &P = h->rp[r];
