@@ -319,7 +319,10 @@ int txg_replot(const txg_replot_opts *opts, const txg_replot_cand *cands, int64_
  * 3 stage 2, 4 boxcar.  Returns the number of classes. */
 int txg_get_timing(txg_handle *h, double *ms, int64_t *launches, int32_t n);
 
-/* The handle's CUDA stream (cudaStream_t) so callers can order or time work against it. */
+/* The handle's CUDA stream (cudaStream_t) so callers can order or time work against it.  The
+ * rows of a block run on streams of their own that fork from this one; their work joins it at
+ * txg_sync and before every call that reads results (txg_get_*), so work queued on it after
+ * txg_sync follows everything pushed before. */
 int txg_get_stream(txg_handle *h, void **stream);
 
 const char *txg_strerror(int32_t status);

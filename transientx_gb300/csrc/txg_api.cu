@@ -233,10 +233,13 @@ struct txg_handle {
     cudaStream_t dst = nullptr; /* device-to-host copies of candidates */
     /* one stream per ddplan row: the rows of a block run concurrently (the single-CTA and
      * latency-bound kernels and the last waves of one row leave SMs to the others); each
-     * forks from the handle stream after the block's shared steps (raw copy, channel zap)
-     * and joins it at the end of the block */
+     * forks from the handle stream after the block's shared steps (raw copy, channel zap),
+     * and the handle stream waits only for every row's unpack before the next block's shared
+     * steps, so consecutive blocks overlap too; readers of results join all rows first */
     std::vector<cudaStream_t> rst;
-    std::vector<cudaEvent_t> row_done;
+    std::vector<cudaEvent_t> row_done;     /* join of everything queued on a row stream */
+    std::vector<cudaEvent_t> row_unpacked; /* a row's unpack (the last reader of the raw block
+                                            * and of the channel-zap mask) is done */
     cudaEvent_t fork = nullptr;
     uint8_t *raw[2] = {nullptr, nullptr};
     uint8_t *stage[2] = {nullptr, nullptr}; /* pinned staging for pageable host input */
@@ -342,8 +345,11 @@ void free_all(txg_handle *h)
         if (s) cudaStreamDestroy(s);
     for (cudaEvent_t e : h->row_done)
         if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : h->row_unpacked)
+        if (e) cudaEventDestroy(e);
     h->rst.clear();
     h->row_done.clear();
+    h->row_unpacked.clear();
     if (h->fork) cudaEventDestroy(h->fork);
     h->fork = nullptr;
     if (h->st) cudaStreamDestroy(h->st);
@@ -487,6 +493,17 @@ long pmod(long a, long m)
     return r < 0 ? r + m : r;
 }
 
+/* The handle stream waits for everything queued so far on the row streams (and so does
+ * whatever is queued on it next). */
+int join_rows(txg_handle *h)
+{
+    for (size_t r = 0; r < h->rst.size(); r++) {
+        TXG_CUDA_TRY(cudaEventRecord(h->row_done[r], h->rst[r]));
+        TXG_CUDA_TRY(cudaStreamWaitEvent(h->st, h->row_done[r], 0));
+    }
+    return TXG_OK;
+}
+
 /* Queue every ddplan row of one block whose raw samples are at `raw` on the device. */
 int run_block(txg_handle *h, int beam, const uint8_t *raw)
 {
@@ -527,6 +544,8 @@ int run_block(txg_handle *h, int beam, const uint8_t *raw)
         float *x = xcur + P.H;
         const bool part = launch_unpack(raw, Craw, n0, P.cfg.td, P.cfg.fd, x, P.ldh, P.C, P.N, mask,
                                         b.eqpart, rs);
+        TXG_CUDA_TRY(cudaEventRecord(h->row_unpacked[r], rs));
+        TXG_CUDA_TRY(cudaStreamWaitEvent(h->st, h->row_unpacked[r], 0));
         if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[1], rs));
 
         /* equalize from the unpack's integer sums; its apply rides on the baseline pass */
@@ -615,8 +634,6 @@ int run_block(txg_handle *h, int beam, const uint8_t *raw)
         b.pushed = counter;
         b.nblocks++;
         if (b.xh[1]) b.cur ^= 1;
-        TXG_CUDA_TRY(cudaEventRecord(h->row_done[r], rs));
-        TXG_CUDA_TRY(cudaStreamWaitEvent(h->st, h->row_done[r], 0));
     }
     return status;
 }
@@ -812,11 +829,13 @@ int txg_create(const txg_plan *plan, txg_handle **out)
     }
     h->rst.assign(plan->nrows, nullptr);
     h->row_done.assign(plan->nrows, nullptr);
+    h->row_unpacked.assign(plan->nrows, nullptr);
     if (cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming) != cudaSuccess)
         return bail(fail(TXG_ERR_CUDA, "event creation failed"));
     for (int r = 0; r < plan->nrows; r++)
         if (cudaStreamCreateWithFlags(&h->rst[r], cudaStreamNonBlocking) != cudaSuccess ||
-            cudaEventCreateWithFlags(&h->row_done[r], cudaEventDisableTiming) != cudaSuccess)
+            cudaEventCreateWithFlags(&h->row_done[r], cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&h->row_unpacked[r], cudaEventDisableTiming) != cudaSuccess)
             return bail(fail(TXG_ERR_CUDA, "row stream creation failed"));
     h->rd.resize(plan->nrows);
     for (int r = 0; r < plan->nrows; r++) {
@@ -948,6 +967,7 @@ int txg_sync(txg_handle *h)
 {
     DeviceScope device_scope(h);
     if (!h) return fail(TXG_ERR_ARG, "null handle");
+    if (int jr = join_rows(h)) return jr; /* results of the row streams */
     TXG_CUDA_TRY(cudaStreamSynchronize(h->st));
     int status = TXG_OK;
     for (auto &beam : h->br)
@@ -1043,6 +1063,7 @@ int txg_get_dense(txg_handle *h, int32_t beam, int32_t row, float *mxS, int32_t 
     if (!(h->flags & TXG_FLAG_DENSE)) return fail(TXG_ERR_STATE, "plan was created without TXG_FLAG_DENSE");
     const RowPlan &P = h->rp[row];
     const BeamRow &b = h->br[beam][row];
+    if (int jr = join_rows(h)) return jr; /* results of the row streams */
     TXG_CUDA_TRY(cudaStreamSynchronize(h->st));
     size_t cnt = (size_t)P.cfg.ndm * P.nout;
     if (mxS) TXG_CUDA_TRY(cudaMemcpy(mxS, b.mxS, cnt * sizeof(float), cudaMemcpyDeviceToHost));
@@ -1057,6 +1078,7 @@ int txg_get_timdata(txg_handle *h, int32_t beam, int32_t row, int64_t idm0, int6
     if (rc) return rc;
     const RowPlan &P = h->rp[row];
     if (!out || idm0 < 0 || count < 0 || idm0 + count > P.cfg.ndm) return fail(TXG_ERR_ARG, "DM range");
+    if (int jr = join_rows(h)) return jr; /* results of the row streams */
     TXG_CUDA_TRY(cudaStreamSynchronize(h->st));
     TXG_CUDA_TRY(cudaMemcpy(out, h->br[beam][row].tim + idm0 * P.nout, count * P.nout * sizeof(float),
                             cudaMemcpyDeviceToHost));
@@ -1122,6 +1144,7 @@ int txg_get_timdata_q(txg_handle *h, int32_t beam, int32_t row, int64_t idm0, in
     if (nsamp < 1 || nsamp > P.nout) return fail(TXG_ERR_ARG, "nsamp must be 1..nsamples");
     if (nbits != 8 && nbits != 16 && nbits != 32) return fail(TXG_ERR_ARG, "nbits must be 8, 16 or 32");
     const size_t bytes = (size_t)count * nsamp * (nbits / 8);
+    if (int jr = join_rows(h)) return jr; /* results of the row streams */
     void *d = nullptr;
     TXG_CUDA_TRY(cudaStreamSynchronize(h->st));
     TXG_CUDA_TRY(cudaMalloc(&d, bytes));
@@ -1144,6 +1167,7 @@ int txg_get_block(txg_handle *h, int32_t beam, int32_t row, float *out)
     const RowPlan &P = h->rp[row];
     const BeamRow &b = h->br[beam][row];
     if (b.nblocks == 0) return fail(TXG_ERR_STATE, "no block pushed");
+    if (int jr = join_rows(h)) return jr; /* results of the row streams */
     TXG_CUDA_TRY(cudaStreamSynchronize(h->st));
     const float *x = (b.xh[1] ? b.xh[b.cur ^ 1] : b.xh[0]) + P.H; /* buffer of the newest block */
     TXG_CUDA_TRY(cudaMemcpy2D(out, P.N * sizeof(float), x, P.ldh * sizeof(float), P.N * sizeof(float), P.C,
@@ -1162,6 +1186,7 @@ int txg_get_zap_ranges(txg_handle *h, int32_t beam, int32_t row, int32_t irfi, i
     const int kind = P.cfg.rfi_kind[irfi];
     if (kind != TXG_RFI_KADANEF && kind != TXG_RFI_KADANET && kind != TXG_RFI_MASK)
         return fail(TXG_ERR_ARG, "rfilist entry is not a kadaneF, kadaneT or mask");
+    if (int jr = join_rows(h)) return jr; /* results of the row streams */
     if (kind == TXG_RFI_MASK) {
         if (!out || cap < 4) return fail(TXG_ERR_ARG, "output too small");
         TXG_CUDA_TRY(cudaStreamSynchronize(h->st));
@@ -1200,6 +1225,7 @@ int txg_get_subdata(txg_handle *h, int32_t beam, int32_t row, int64_t idm, float
     if (rc) return rc;
     const RowPlan &P = h->rp[row];
     if (!out || idm < 0 || idm >= P.cfg.ndm) return fail(TXG_ERR_ARG, "DM index or output");
+    if (int jr = join_rows(h)) return jr; /* results of the row streams */
     const size_t cnt = (size_t)P.nsub * P.nout;
     float *d = nullptr;
     TXG_CUDA_TRY(cudaMalloc(&d, cnt * sizeof(float)));
@@ -1226,6 +1252,7 @@ int txg_cand_band(txg_handle *h, int32_t beam, int32_t row, const txg_cand *c, i
     for (long k = 0; k < n; k++)
         if (c[k].idm < 0 || c[k].idm >= P.cfg.ndm || c[k].wn < 1)
             return fail(TXG_ERR_ARG, "candidate outside the row");
+    if (int jr = join_rows(h)) return jr; /* results of the row streams */
     std::vector<float> vpf((size_t)n * P.nsub);
     txg_cand *dc = nullptr;
     float *dv = nullptr;
@@ -1273,6 +1300,7 @@ int txg_get_mask(txg_handle *h, int32_t beam, uint8_t *mask)
     DeviceScope device_scope(h);
     if (!h || !mask) return fail(TXG_ERR_ARG, "null argument");
     if (beam < 0 || beam >= (int)h->prep.size()) return fail(TXG_ERR_ARG, "beam out of range");
+    if (int jr = join_rows(h)) return jr; /* results of the row streams */
     TXG_CUDA_TRY(cudaStreamSynchronize(h->st));
     TXG_CUDA_TRY(cudaMemcpy(mask, h->prep[beam].mask, h->plan.nchans, cudaMemcpyDeviceToHost));
     return TXG_OK;
