@@ -86,7 +86,8 @@ struct Result {
     std::vector<txg_cand> cands;   /* (idm, isamp) order */
     std::vector<txg_cand> clusters;
     bool failed = false;
-    bool ready = false; /* guarded by Workers::m */
+    bool released = false; /* the pinned read-back is read no more (guarded by Workers::m) */
+    bool ready = false;    /* guarded by Workers::m */
 };
 using ResultP = std::shared_ptr<Result>;
 
@@ -142,7 +143,20 @@ struct Workers {
     void complete(Result &r) /* a result with nothing to do on a worker */
     {
         std::lock_guard<std::mutex> lk(m);
-        r.ready = true;
+        r.released = r.ready = true;
+    }
+    void release(Result &r) /* the job has copied its points out of the pinned read-back */
+    {
+        {
+            std::lock_guard<std::mutex> lk(m);
+            r.released = true;
+        }
+        done.notify_all();
+    }
+    void wait_released(const Result &r)
+    {
+        std::unique_lock<std::mutex> lk(m);
+        done.wait(lk, [&] { return r.released || r.ready; });
     }
     void wait(const Result &r)
     {
@@ -393,11 +407,12 @@ void sort_points(const txg_cand *a, long na, const txg_cand *b, long nb, long nd
 }
 
 /* Host side of one harvested block (on a worker thread): sort its points, cluster them. */
-void post_process(const txg_handle *h, const RowPlan &P, Result &r)
+void post_process(const txg_handle *h, const RowPlan &P, Result &r, Workers *pool)
 {
     try {
         sort_points(r.src, r.nsrc, r.tail.data(), (long)r.tail.size(), P.cfg.ndm, P.nout, r.cands);
         r.src = nullptr;
+        pool->release(r); /* the slot's pinned buffer may take the next block now */
         std::vector<txg_cand>().swap(r.tail);
         if ((h->flags & TXG_FLAG_CLUSTER) && r.gated && !r.cands.empty()) {
             const txg_row &c = P.cfg;
@@ -411,6 +426,7 @@ void post_process(const txg_handle *h, const RowPlan &P, Result &r)
         r.failed = true;
         r.cands.clear();
         r.clusters.clear();
+        pool->release(r);
     }
 }
 
@@ -479,7 +495,7 @@ int harvest(txg_handle *h, BeamRow &b, Slot &sl, const RowPlan &P)
     const RowPlan *pp = &P;
     if (r->nsrc > 0 || !r->tail.empty())
         pool->submit([h, pool, pp, r] {
-            post_process(h, *pp, *r);
+            post_process(h, *pp, *r, pool);
             pool->finish(*r);
         });
     else
@@ -609,8 +625,8 @@ int run_block(txg_handle *h, int beam, const uint8_t *raw)
              * count of candidates (the rest, if any, is fetched at harvest) and the count.
              * The buffer's previous reader (two uses of this slot ago) must be done. */
             sl.buf = (int)(sl.uses++ & 1);
-            if (sl.reader[sl.buf]) {
-                h->pool->wait(*sl.reader[sl.buf]);
+            if (sl.reader[sl.buf]) { /* its previous block's sort must have read it */
+                h->pool->wait_released(*sl.reader[sl.buf]);
                 sl.reader[sl.buf].reset();
             }
             sl.nread = std::min(b.guess, h->hcap);
