@@ -21,7 +21,7 @@
  *                                            include/clustering.h:26-100
  * Equalize, BaseLine, RFI::zdot/kadaneF of the main path and RealTime::SubbandDedispersion
  * live in the external XLibs library, which is not part of the reference tree: their
- * definitions here follow the reference documentation (docs/pipeline/*.rst) and the
+ * definitions here follow the reference documentation (the rst files of docs/pipeline) and the
  * in-tree candidate.cpp versions; parity for those stages is "unpinned" against XLibs.
  */
 #ifndef TXORACLE_H
