@@ -4,7 +4,7 @@
  * zdot) -> two-stage subband dedispersion -> boxcar matched filter -> S/N threshold.
  *
  * Plain C types only; every function returns a txg_status (0 = success, < 0 = error) unless
- * noted.  One handle owns its device memory and CUDA stream; calls on one handle must be
+ * noted.  One handle owns its device memory and CUDA streams; calls on one handle must be
  * serialised by the caller, different handles are independent.  A handle lives on the CUDA
  * device current at txg_create; each call on it makes that device current for the call and
  * restores the caller's.  No exceptions cross this boundary.  Paths below are relative to
