@@ -1,7 +1,7 @@
 /*
  * txoracle.c -- CPU restatement of the TransientX per-block single-pulse hot path.
  *
- * TEST INFRASTRUCTURE ONLY (the checker and the timed CPU baseline).  The product never
+ * TEST INFRASTRUCTURE ONLY (the oracle of the tests and the timed CPU baseline).  The product never
  * links or calls this file.  Build with -ffp-contract=off: every floating-point operation
  * below is meant to round exactly once, as written.
  *

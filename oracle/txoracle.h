@@ -1,8 +1,8 @@
 /*
  * txoracle.h -- CPU restatement of the TransientX per-block single-pulse hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker the CUDA path is compared against
- * and the timed CPU baseline of bench.py.  The product library (transientx_gb300) never
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle the CUDA path is compared against in
+ * the tests and the timed CPU baseline of bench.py.  The product library (transientx_gb300) never
  * links, loads or calls it.
  *
  * What is restated from where (paths relative to the TransientX source tree):

@@ -149,7 +149,7 @@ def nchan4096_rfi(seed: int = 2, nsamples: int = 1 << 21) -> Workload:
 
 
 def nchan8192_dm5000(seed: int = 5, nsamples: int = 1 << 23) -> Workload:
-    """One beam of the 8192-channel survey shape: 1200-1800 MHz, 16 us, 2^23 samples (134 s),
+    """One beam of an 8192-channel search-mode observation: 1200-1800 MHz, 16 us, 2^23 samples (134 s),
     RFI as the 4096-channel workload (5% sinusoid channels, zero-DM impulses at 1/s), bursts of
     32 us-5 ms at DM 10-5000 and S/N 8-30.  Five ddplan rows to DM 5000 with td 1/2/4/8/16,
     maxw 0.01 s, rfilist kadaneF 8 4, zdot; 1 s blocks (62496 samples at td 1)."""
