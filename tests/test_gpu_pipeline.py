@@ -79,6 +79,59 @@ def test_pipeline_fp32_matches_oracle(tx, oracle, avx2, zapthre):
     assert ngated >= 4
 
 
+EDGE_CASES = {
+    # name: (nchans, tsamp, ndump, row keyword arguments)
+    "tiny_one_dm": (16, 256e-6, 64, dict(td=1, fd=1, dms=30.0, ddm=1.0, ndm=1, maxw=0.002,
+                                          rfilist=[["zdot"]], bswidth=0.005)),
+    "odd_channels_fd3": (33, 256e-6, 768, dict(td=2, fd=3, dms=0.0, ddm=2.0, ndm=40, maxw=0.01,
+                                               rfilist=[["kadaneF", "3", "2"], ["zdot"]],
+                                               widthlimit=0.005, bswidth=0.05)),
+    "ragged_kadane_cells": (96, 128e-6, 1000, dict(td=1, fd=1, dms=10.0, ddm=0.5, ndm=64, maxw=0.01,
+                                                   rfilist=[["kadaneF", "7", "5"]], widthlimit=0.003,
+                                                   bswidth=0.02, nsub=8)),
+    "one_width": (64, 256e-6, 512, dict(td=1, fd=1, dms=0.0, ddm=1.0, ndm=32, minw=2.5e-4,
+                                        maxw=3e-4, bswidth=0.0)),
+}
+
+
+@pytest.mark.parametrize("name", list(EDGE_CASES))
+def test_edge_geometries_match_oracle(tx, oracle, name):
+    """Edge geometries: a 64-sample block with one DM, 33 channels downsampled by 3 (the staged
+    unpack), kadaneF cells that do not divide the block, a one-width ladder.  Blocks, zap
+    windows and series bit-exact, boxcar within the tolerance, every block."""
+    from transientx_gb300 import SinglePulse, synth
+    C, tsamp, ndump, kw = EDGE_CASES[name]
+    f = synth.band(C, 1500.0, 1300.0)
+    T = 12 * ndump * tsamp
+    fil = synth.Filterbank(C, tsamp, f, 12 * ndump, 13, pulses=[(0.6 * T, 40.0, 4 * tsamp, 30.0)],
+                           sines=[(C // 3, 20.0, 0.01, 0.2)])
+    rows = [SinglePulse(**kw)]
+    flags = tx.FLAG_DENSE | tx.FLAG_KEEP_SERIES
+    o = oracle_rows(oracle, rows, fil, ndump, tx)[0]
+    ngated = 0
+    with tx.Search(rows, C, tsamp, f, ndump, flags=flags, zapthre=4.0) as s:
+        for b in range(12):
+            raw = fil.generate(b * ndump, ndump)
+            s.push_block(raw)
+            s.sync()
+            gated = o.run(raw)
+            assert bool(s.row_info(0).gated) == gated
+            np.testing.assert_array_equal(s.block(0), o.block(), err_msg=f"{name} block {b}")
+            for q, op in enumerate(rows[0].rfilist):
+                if op[0] == "kadaneF":
+                    np.testing.assert_array_equal(s.zap_ranges(q, 0), o.zap_ranges(q))
+            if not gated:
+                continue
+            ngated += 1
+            tim = s.timdata(0)
+            np.testing.assert_array_equal(tim, o.timdata(), err_msg=f"{name} tim {b}")
+            S, W = s.dense(0)
+            assert_boxcar_close(tim, o.widths(), S, W, o.mxS(), o.mxwn())
+            ref = oracle.threshold_scan(o.mxS(), o.mxwn(), rows[0].thre)
+            assert_cands_close(s.candidates(0), ref, rows[0].thre)
+    assert ngated >= 1
+
+
 RFI_LISTS = {
     "mask": [["mask", "4", "2"]],
     "mask11": [["mask", "1", "1"]],
