@@ -412,3 +412,60 @@ def test_snr_error_against_fp64_oracle(tx, oracle, prec, bound):
     print(f"{prec}: {npts} points above threshold, max relative S/N error {worst:.2e}")
     if bound is not None:
         assert worst <= bound, (prec, worst)
+
+
+@pytest.mark.parametrize("prec,pinned,nbeams", [("fp32", False, 1), ("fp32", True, 1),
+                                                ("fp16", False, 1), ("fp32", False, 2)])
+def test_streamed_blocks_equal_synced_blocks(tx, prec, pinned, nbeams):
+    """Blocks pushed back to back (the device runs up to three blocks ahead, the rows of a
+    block run on their own streams, candidate slots are reused while earlier blocks are still
+    being clustered, beams interleave) give, block by block, the same points and clusters as
+    pushing one block and waiting for it.  Pinned inputs are copied asynchronously, so each
+    block keeps its own buffer until the sync."""
+    import torch
+    fil, rows, ndump = small_workload()
+    nblk = fil.nsamples // ndump
+    raws = [fil.generate(b * ndump, ndump) for b in range(nblk)]
+    if pinned:
+        bufs = [torch.empty(r.shape, dtype=torch.uint8, pin_memory=True) for r in raws]
+        for t, r in zip(bufs, raws):
+            t.numpy()[...] = r
+        inputs = [t.numpy() for t in bufs]
+    else:
+        inputs = raws
+
+    def drain(s, beam, out):
+        for r in range(len(rows)):
+            while True:
+                got = s.pop_result(r, beam)
+                if got is None:
+                    break
+                res, pts, cl = got
+                out[r].append((res.counter, res.gated, pts, cl))
+
+    kw = dict(flags=tx.FLAG_CLUSTER, precision=prec)
+    ref = [[] for _ in rows]
+    with tx.Search(rows, fil.nchans, fil.tsamp, fil.freqs, ndump, **kw) as a:
+        for raw in raws:
+            a.push_block(raw)
+            a.sync()
+            drain(a, 0, ref)
+    streamed = [[[] for _ in rows] for _ in range(nbeams)]
+    with tx.Search(rows, fil.nchans, fil.tsamp, fil.freqs, ndump, nbeams=nbeams, **kw) as b:
+        for x in inputs:
+            for beam in range(nbeams):
+                b.push_block(x, beam=beam)
+        b.sync()
+        for beam in range(nbeams):
+            drain(b, beam, streamed[beam])
+    npts = 0
+    for beam in range(nbeams):
+        for r in range(len(rows)):
+            assert len(ref[r]) == len(streamed[beam][r]) == nblk
+            for blk, (u, v) in enumerate(zip(ref[r], streamed[beam][r])):
+                where = f"beam {beam} row {r} block {blk}"
+                assert u[:2] == v[:2], where
+                np.testing.assert_array_equal(u[2], v[2], err_msg=where + " points")
+                np.testing.assert_array_equal(u[3], v[3], err_msg=where + " clusters")
+                npts += len(u[2])
+    assert npts > 0, "the injected pulses should give points above threshold"
