@@ -301,10 +301,19 @@ k_stage1r(const float *__restrict__ xh, long ldh, long col0, int C, long N, int 
                 dd[4 * gq + 2] = d.z;
                 dd[4 * gq + 3] = d.w;
             }
+            /* neighbouring coarse-DM groups often share a channel's delay (it moves by a
+             * third of a sample per group on average): the window values are loaded again only
+             * where the delay changes (a branch uniform over the thread set) */
+            float v[U];
 #pragma unroll
-            for (int g = 0; g < GPT; g++)
+            for (int g = 0; g < GPT; g++) {
+                if (g == 0 || dd[g] != dd[g - 1]) {
 #pragma unroll
-                for (int q = 0; q < U; q++) acc[g][q] = __fadd_rn(acc[g][q], wr[dd[g] + q * TH]);
+                    for (int q = 0; q < U; q++) v[q] = wr[dd[g] + q * TH];
+                }
+#pragma unroll
+                for (int q = 0; q < U; q++) acc[g][q] = __fadd_rn(acc[g][q], v[q]);
+            }
         }
 #pragma unroll
         for (int g = 0; g < GPT; g++) {
@@ -444,11 +453,17 @@ k_stage1p(const __half *__restrict__ xh, long ldh, long col0, int C, long N, int
                 dd[4 * gq + 2] = d.z;
                 dd[4 * gq + 3] = d.w;
             }
+            /* window words loaded again only where the delay changes, as in k_stage1r */
+            uint32_t v[UP];
 #pragma unroll
-            for (int g = 0; g < GPT; g++)
+            for (int g = 0; g < GPT; g++) {
+                if (g == 0 || dd[g] != dd[g - 1]) {
 #pragma unroll
-                for (int q = 0; q < UP; q++)
-                    addp(acc[g][2 * q], acc[g][2 * q + 1], wr[dd[g] + q * TH], __half());
+                    for (int q = 0; q < UP; q++) v[q] = wr[dd[g] + q * TH];
+                }
+#pragma unroll
+                for (int q = 0; q < UP; q++) addp(acc[g][2 * q], acc[g][2 * q + 1], v[q], __half());
+            }
         }
 #pragma unroll
         for (int g = 0; g < GPT; g++) {
@@ -835,10 +850,11 @@ static void stage1_chunked(const float *xh, long ldh, long col0, int C, long N, 
  *                 4 = 256x1 4x4, 5 = 128x1 4x8, 6 = 256x1 4x8, 7 = 64x4 8x4, 8 = 128x2 8x4,
  *                 9 = 64x4 16x4, 10 = 128x2 4x8, 11 = 64x8 8x4
  * Every channel step loads the thread's delays (broadcast 16-byte loads, two shared-memory
- * wavefronts each) and then one window element per sample per group: many samples per thread
- * and one warp per set keep the delay loads a small share of the shared-memory traffic
- * (measured on the 4096-channel workload: 32x16 16x4 took stage 1 from 185 to 159 ms per 20
- * blocks against 256x2 4x8).  A shape whose windows do not fit falls back to 256x2 1x16, then
+ * wavefronts each) and then one window element per sample for each distinct delay among its
+ * groups: many samples per thread and one warp per set keep the delay loads a small share of
+ * the shared-memory traffic (measured on the 4096-channel workload: 32x16 16x4 took stage 1
+ * from 185 to 159 ms per 20 blocks against 256x2 4x8; loading only where the delay changes,
+ * 159 to 114 ms FP32 and 111 to 102 ms for the 16-bit pairs).  A shape whose windows do not fit falls back to 256x2 1x16, then
  * to the chunked kernel (any negative variant selects the chunked kernel directly).  The
  * 16-bit fallbacks past the pair kernels read the FP32 block (one rounding fewer than the FP16
  * copy), so their series can differ in the last bits from the pair kernels'. */
