@@ -127,13 +127,28 @@ SMEM_BYTES_PER_CLK = 128  # shared-memory bytes one SM delivers per clock
 NSM = 152
 
 
-def class_smem_bytes(info, elem):
-    """Shared-memory bytes a perfect implementation must load for one launch of the classes
-    bound by shared memory: stage 1 loads one window element per addition (C x ngroup x N
-    additions), stage 2 likewise (nsub x ndm x (N + noverlap)), the boxcar two running-sum
-    values per (sample, width).  Other classes: None."""
-    N, C = info.ndump, info.nchans
-    return [None, None, float(elem) * C * info.ngroup * N,
+S1_SETS, S1_GPT = 16, 4  # default stage-1 shapes: 16 thread sets of 4 coarse-DM groups per CTA
+
+
+def stage1_window_loads(d1):
+    """Window elements stage 1 loads per output sample, summed over channels and thread sets,
+    at the default launch shapes: a thread set loads a channel's window values for its first
+    group and again wherever the delay differs from the previous group's (groups past the end
+    repeat the last delay)."""
+    ng, C = d1.shape
+    gpc = S1_SETS * S1_GPT
+    nch = (ng + gpc - 1) // gpc
+    pad = np.concatenate([d1, np.repeat(d1[-1:], nch * gpc - ng, axis=0)]).reshape(-1, S1_GPT, C)
+    return int(pad.shape[0] * C + (pad[:, 1:] != pad[:, :-1]).sum())
+
+
+def class_smem_bytes(info, elem, d1):
+    """Shared-memory bytes one launch of the classes bound by shared memory loads: stage 1 one
+    window element per sample for each delay change within a thread set's groups (the loads
+    the kernel makes; additions are C x ngroup x N), stage 2 one window element per addition
+    (nsub x ndm x (N + noverlap)), the boxcar two running-sum values per (sample, width).
+    Other classes: None."""
+    return [None, None, float(elem) * info.ndump * stage1_window_loads(d1),
             float(elem) * info.nsub * info.ndm * info.nsamples,
             8.0 * info.ndm * info.nsamples * info.nwidths]
 
@@ -329,7 +344,8 @@ def run_ours(args, wl):
             nb_total[c] += cb[c] * (tsteps * nblk if c < 3 else nblocks_r)
     sm_total = [0.0] * 5
     for r, (sp, info) in enumerate(zip(wl.rows, infos)):
-        sb = class_smem_bytes(info, ELEM[args.precision])
+        d1 = tx.describe_row(wl.rows, r, fil.nchans, fil.tsamp, fil.freqs, wl.ndump)[1]
+        sb = class_smem_bytes(info, ELEM[args.precision], d1)
         for c in (2, 3, 4):
             sm_total[c] += sb[c] * (tsteps * nblk if c < 3 else tstats["gated"][r])
     peak, peak_kind = measured_peaks()
@@ -353,8 +369,10 @@ def run_ours(args, wl):
         sm_ach = sm_total[top] / (cls_ms[top] / 1e3) / 1e12
         roof["smem"] = {"achieved": sm_ach, "peak": sm_peak, "unit": "TB/s", "frac": sm_ach / sm_peak,
                         "peak_basis": f"{NSM} SMs x {SMEM_BYTES_PER_CLK} B/clock x median SM clock",
-                        "basis": "one shared-memory window element per addition (stages 1, 2), "
-                                 "two running-sum loads per sample and width (boxcar)"}
+                        "basis": "window elements loaded: stage 1 one per sample for each delay "
+                                 "change within a thread set's coarse-DM groups (default shapes), "
+                                 "stage 2 one per addition; two running-sum loads per sample and "
+                                 "width (boxcar)"}
 
     s.close()
     e2e = None
