@@ -176,3 +176,31 @@ def test_no_device_is_reported(tx):
     with pytest.raises(TxgError) as e:
         boxcar(np.zeros((2, 64), np.float32), [2, 3])
     assert e.value.status == tx.ERR_NODEVICE
+
+
+@pytest.mark.parametrize("descending", [True, False])
+def test_stage1_delays_grow_with_the_group(tx, descending):
+    """The stage-1 kernels size each subband's shared-memory window by the last coarse-DM
+    group's delays: every delay is >= 0, never decreases from one group to the next, and the
+    last group holds each channel's largest (and maxd1 is the largest overall).  Stage 2 sizes
+    a chunk's subband window by its first and last fine DM's offsets, so the subband delays
+    never decrease with the DM either.  Checked for bands in either frequency order, partial
+    last groups and DM ranges starting above 0."""
+    from transientx_gb300 import SinglePulse, synth
+    rng = np.random.default_rng(5)
+    for C, fhi, flo, ts, dms, ddm, ndm, G in [(4096, 1712.0, 856.0, 76e-6, 0.0, 0.1, 5000, 0),
+                                                (256, 1500.0, 1244.0, 64e-6, 0.0, 0.5, 2000, 0),
+                                                (8192, 1800.0, 1200.0, 16e-6, 700.0, 0.5, 2000, 0),
+                                                (100, 400.0, 300.0, 1e-3, 3.0, 0.37, 77, 5),
+                                                (33, 1400.0, 1390.0, 1e-4, 0.0, 2.0, 9, 4)]:
+        f = synth.band(C, fhi, flo)
+        if not descending:
+            f = f[::-1].copy()
+        sp = SinglePulse(dms=dms, ddm=ddm, ndm=ndm, dm_group=G, nsub=int(rng.integers(0, 2)) * 8)
+        info, d1, d2 = tx.describe_row([sp], 0, C, ts, f, 4096)[:3]
+        assert (d2 >= 0).all() and (np.diff(d2, axis=0) >= 0).all()
+        assert info.maxd2 == d2.max()
+        assert (d1 >= 0).all()
+        assert (np.diff(d1, axis=0) >= 0).all(), (C, descending)
+        np.testing.assert_array_equal(d1[-1], d1.max(axis=0))
+        assert info.maxd1 == d1.max()
