@@ -130,8 +130,9 @@ void txg_destroy(txg_handle *h);
 /* Feed one block of raw uint8 time-major samples [nsamp][nchans] for one beam and run every
  * ddplan row on it: the body of the transientx_fil block loop (dedisperse_fil.cpp:324-337)
  * calling SinglePulse::run (singlepulse.cpp:287-341).  nsamp must equal the plan's ndump.
- * The host variant copies through pinned staging buffers; the call returns once the block
- * is queued and the caller's buffer may be reused. */
+ * The call returns once the block is queued.  A pageable host buffer is first copied into a
+ * pinned staging buffer and may be reused on return; a page-locked host buffer is copied to
+ * the device asynchronously and must stay unchanged until the next txg_sync. */
 int txg_push_block(txg_handle *h, int32_t beam, const uint8_t *host, int64_t nsamp);
 int txg_push_block_device(txg_handle *h, int32_t beam, const uint8_t *dev, int64_t nsamp);
 
