@@ -9,6 +9,8 @@
  *                         run(block) (the block-loop body, dedisperse_fil.cpp:324-337)
  *   txgpu::Search::cluster - Cluster<double>::run's candlist (cluster.cpp:63-161) as
  *                         (idm, isamp, wn, S) tuples, the order CandPlot::plot consumes
+ *   txgpu::Boxcar       - the public members of Boxcar (include/boxcar.h:31-43) for one row
+ *                         after its last block (Search::boxcar), with dump2txt
  * Errors from the C ABI become txgpu::Error exceptions on the C++ side only.
  */
 #ifndef TRANSIENTX_GB300_HPP
@@ -215,6 +217,40 @@ private:
     long num_cand_ = 0;
 };
 
+/* The public members of the reference's Boxcar (include/boxcar.h:31-43) for one (row, beam)
+ * after its last block, as Search::boxcar fills them.  mxS / mxwn are the dense
+ * [ndm][nsamples] planes when the plan has TXG_FLAG_DENSE and stay empty otherwise (the GPU
+ * path feeds clustering from the compacted points instead); gated is what Boxcar::run
+ * returned (boxcar.cpp:160-161).  finterval and match2D (marked "not work",
+ * boxcar.cpp:298) are not carried. */
+struct Boxcar {
+    long counter = 0;
+    double tsamp = 0.;
+    long nsamples = 0;
+    double dms = 0., ddm = 0.;
+    long ndm = 0;
+    int maxwn = 0;
+    double fmin = 0., fmax = 0.;
+    std::vector<float> mxS;
+    std::vector<int> mxwn;
+    bool gated = false;
+
+    /* mxS as text, one line per DM trial, each value printed "%f " (boxcar.cpp:473-489) */
+    void dump2txt(const std::string &fname) const
+    {
+        if (mxS.size() != (size_t)ndm * (size_t)nsamples)
+            throw Error(TXG_ERR_STATE, "dump2txt: no dense mxS (plan without TXG_FLAG_DENSE)");
+        FILE *f = std::fopen(fname.c_str(), "w");
+        if (!f) throw Error(TXG_ERR_ARG, "dump2txt: cannot open " + fname);
+        const float *p = mxS.data();
+        for (long j = 0; j < ndm; j++) {
+            for (long i = 0; i < nsamples; i++) std::fprintf(f, "%f ", *p++);
+            std::fprintf(f, "\n");
+        }
+        std::fclose(f);
+    }
+};
+
 class Search {
 public:
     Search(const std::vector<SinglePulse> &rows, int nchans, double tsamp,
@@ -237,6 +273,7 @@ public:
         p.zapthre = zapthre;
         check(txg_create(&p, &h_), "txg_create");
         ndump_ = ndump;
+        flags_ = flags;
     }
     ~Search() { txg_destroy(h_); }
     Search(const Search &) = delete;
@@ -286,6 +323,29 @@ public:
         return list;
     }
 
+    /* Boxcar's members for the row's last block; the dense planes with TXG_FLAG_DENSE */
+    Boxcar boxcar(int row, int beam = 0) const
+    {
+        const txg_row_info i = info(row, beam);
+        Boxcar b;
+        b.counter = (long)i.counter;
+        b.tsamp = i.tsamp;
+        b.nsamples = (long)i.nsamples;
+        b.dms = i.dms;
+        b.ddm = i.ddm;
+        b.ndm = (long)i.ndm;
+        b.maxwn = i.maxwn;
+        b.fmin = i.fmin;
+        b.fmax = i.fmax;
+        b.gated = i.gated != 0;
+        if (flags_ & TXG_FLAG_DENSE) {
+            b.mxS.resize((size_t)i.ndm * (size_t)i.nsamples);
+            b.mxwn.resize(b.mxS.size());
+            check(txg_get_dense(h_, beam, row, b.mxS.data(), b.mxwn.data()), "txg_get_dense");
+        }
+        return b;
+    }
+
     /* fl, fh of each candidate of the row's last block (for CandsWriter) */
     void band(int row, const std::vector<txg_cand> &c, std::vector<float> &fl, std::vector<float> &fh,
               int beam = 0) const
@@ -306,6 +366,7 @@ private:
     std::vector<SinglePulse> rows_;
     txg_handle *h_ = nullptr;
     long ndump_ = 0;
+    int flags_ = 0;
 };
 
 } // namespace txgpu

@@ -20,7 +20,20 @@ int main(int argc, char **argv) {
     for (int j = 0; j < C; j++) f[j] = 1500.0 - (j + 0.5) * 300.0 / C;
     auto rows = txgpu::parse_ddplan("# td fd dms ddm ndm snrloss maxw\n1 1 0 1 100 0.1 0.02\n");
     rows[0].nsub = 8;
-    if (argc < 2) { std::printf("parsed %zu rows\n", rows.size()); return 0; }
+    if (argc < 2) {
+        std::printf("parsed %zu rows\n", rows.size());
+        txgpu::Boxcar bx;                 /* Boxcar::dump2txt on host-filled planes */
+        bx.ndm = 3;
+        bx.nsamples = 4;
+        for (int k = 0; k < 12; k++) bx.mxS.push_back(k * 1.25f - 3.5f);
+        bx.dump2txt("boxcar.txt");
+        txgpu::Boxcar none;
+        none.ndm = 2;
+        none.nsamples = 2;
+        try { none.dump2txt("never.txt"); std::printf("no throw\n"); }
+        catch (const txgpu::Error &e) { std::printf("throws %d\n", e.status); }
+        return 0;
+    }
     txgpu::Search s(rows, C, tsamp, f, N);
     std::vector<uint8_t> raw(N * C);
     unsigned long long z = 12345;
@@ -61,8 +74,15 @@ def _compile(tmp_path):
 
 def test_header_compiles_and_parses(tmp_path):
     exe = _compile(tmp_path)
-    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True,
+                         cwd=tmp_path).stdout
     assert "parsed 1 rows" in out
+    # Boxcar::dump2txt: one line per DM trial, "%f " per value (boxcar.cpp:473-489)
+    vals = np.arange(12, dtype=np.float32) * np.float32(1.25) - np.float32(3.5)
+    want = "".join("".join("%f " % v for v in vals[j * 4:(j + 1) * 4]) + "\n" for j in range(3))
+    assert (tmp_path / "boxcar.txt").read_text() == want
+    # without dense planes it refuses (TXG_ERR_STATE) instead of reading nothing
+    assert "throws -6" in out
 
 
 @pytest.mark.gpu
