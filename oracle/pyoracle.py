@@ -480,6 +480,9 @@ def ref_lib(variant="scalar") -> C.CDLL:
                              C.c_void_p, C.c_long, C.POINTER(C.c_long), C.POINTER(C.c_int),
                              C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_double),
                              C.POINTER(C.c_double), C.c_void_p, C.c_long, C.POINTER(C.c_int)]
+    L.ref_candidate_rfi.restype = C.c_int
+    L.ref_candidate_rfi.argtypes = [f32p, C.c_int, C.c_long, C.c_double, C.c_float, C.c_int,
+                                    C.c_int, C.c_int, C.c_float, C.c_int, C.c_void_p]
     L.ref_cluster_run.restype = C.c_long
     L.ref_cluster_run.argtypes = [f32p, i32p, C.c_long, C.c_long, C.c_double, C.c_double,
                                   C.c_double, C.c_double, C.c_double, C.c_int, C.c_float,
@@ -518,6 +521,23 @@ def ref_replot(data, freqs, tbin, dm, width, zdot=False, kadane=None, clip=None,
         res.update(snr=np.float32(snr.value), width=np.float32(wid.value), dm_maxsnr=dmx.value,
                    mjd=mjd.value, ndm=nd.value, snrmap=smap[:nd.value * nb.value].reshape(nd.value, nb.value))
     return res
+
+
+def ref_zdot(x, variant="scalar"):
+    """The reference's Candidate::zdot (candidate.cpp:831-897) on a [nchan][nbin] block."""
+    x = np.array(x, np.float32, order="C")
+    ref_lib(variant).ref_candidate_rfi(x, x.shape[0], x.shape[1], 1.0, 1.0, 0, 1, 1, 0.0, 1, None)
+    return x
+
+
+def ref_kadaneF(x, td, fd, threshold, nwidth, width, tbin, variant="scalar"):
+    """The reference's Candidate::get_stats + normalize + kadaneF(td, fd, threshold, nwidth)
+    (candidate.cpp:429-567, 710-829) on a [nchan][nbin] block: (normalised block, result)."""
+    x = np.array(x, np.float32, order="C")
+    pre = np.zeros_like(x)
+    ref_lib(variant).ref_candidate_rfi(x, x.shape[0], x.shape[1], tbin, width, 1, td, fd,
+                                       threshold, nwidth, pre.ctypes.data)
+    return pre, x
 
 
 def ref_boxcar_run(tim, vwn, iqr=False, variant="scalar", nthreads=4):

@@ -1,0 +1,42 @@
+/*
+ * ref_rfi.cpp -- extern "C" entry around the reference's own Candidate::zdot and
+ * Candidate::kadaneF (src/singlepulse/candidate.cpp:710-897, compiled in place), run on a
+ * channel-major block [nchan][nbin], so that the oracle's main-path restatements (txo_zdot,
+ * txo_kadaneF) can be compared with the in-tree code they follow.  Test infrastructure only.
+ *
+ * op 0: zdot on the block as given.
+ * op 1: get_stats + normalize (Candidate::kadaneF refuses unnormalised data,
+ *       candidate.cpp:712-716), the normalised block copied to `normalized`, then
+ *       kadaneF(td, fd, threshold, nwidth) with the candidate width `width` and bin `tbin`.
+ * The block is overwritten with the result.
+ */
+#include <cstring>
+
+#include "candidate.h"
+
+extern unsigned int num_threads;
+
+extern "C" int ref_candidate_rfi(float *data, int nchan, long nbin, double tbin, float width, int op,
+                                 int td, int fd, float threshold, int nwidth, float *normalized)
+{
+    num_threads = 1;
+    Candidate c;
+    c.npol = 1;
+    c.nchan = nchan;
+    c.nbin = nbin;
+    c.tbin = tbin;
+    c.width = c.width_orig = width;
+    c.data.assign(data, data + (size_t)nchan * nbin);
+    if (op == 0) {
+        c.zdot();
+    } else if (op == 1) {
+        c.get_stats();
+        c.normalize();
+        if (normalized) std::memcpy(normalized, c.data.data(), sizeof(float) * (size_t)nchan * nbin);
+        c.kadaneF(td, fd, threshold, nwidth);
+    } else {
+        return -1;
+    }
+    std::memcpy(data, c.data.data(), sizeof(float) * (size_t)nchan * nbin);
+    return 0;
+}

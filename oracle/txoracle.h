@@ -22,7 +22,9 @@
  * Equalize, BaseLine, RFI::zdot/kadaneF of the main path and RealTime::SubbandDedispersion
  * live in the external XLibs library, which is not part of the reference tree: their
  * definitions here follow the reference documentation (the rst files of docs/pipeline) and the
- * in-tree candidate.cpp versions; parity for those stages is "unpinned" against XLibs.
+ * in-tree candidate.cpp versions; parity for those stages is "unpinned" against XLibs.  The
+ * zdot and kadaneF restatements are compared with the reference's own Candidate::zdot and
+ * Candidate::kadaneF compiled in place (ref_rfi.cpp).
  */
 #ifndef TXORACLE_H
 #define TXORACLE_H

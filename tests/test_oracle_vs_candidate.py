@@ -1,0 +1,58 @@
+"""The oracle's main-path zdot and kadaneF (oracle/txoracle.c, the restatements the GPU kernels
+equal bit for bit) against the reference's own Candidate::zdot and Candidate::kadaneF
+(src/singlepulse/candidate.cpp:710-897, compiled in place with oracle/ref_rfi.cpp), the
+in-tree code the main path's XLibs RFI::zdot / RFI::kadaneF are restated from.  Both sides
+use the project's kadane<float> (oracle/refshim/utils.h: XLibs' version is not in the tree).
+
+kadaneF: bit-exact on the normalised block Candidate::kadaneF sees, with the main path's
+squared threshold and the window limit Candidate computes.  zdot: the oracle folds its sums
+in FP32 runs of 32 with FP64 accumulators (the GPU's order) where Candidate adds sequentially
+in FP64, so values agree within 2e-5 of the block's largest magnitude (observed: 5e-7)."""
+import numpy as np
+import pytest
+
+
+@pytest.fixture(scope="module")
+def ref(oracle):
+    if not oracle.ref_available("scalar"):
+        pytest.skip("reference tree not present")
+    return oracle
+
+
+def _block(C, n, seed):
+    rng = np.random.default_rng(seed)
+    x = rng.normal(3.0, 2.0, (C, n)).astype(np.float32)
+    x[min(5, C - 1)] = 7.0                                # a constant channel (std 0 -> 1)
+    x[:, n // 10:n // 10 + 10] += 5.0                     # a broadband burst
+    x[:: max(1, C // 8), :] += np.float32(2.0) * np.sin(np.arange(n) / 9.0).astype(np.float32)
+    return x
+
+
+@pytest.mark.parametrize("C,n,seed", [(64, 1000, 1), (128, 4096, 2), (33, 517, 3), (1, 64, 4)])
+def test_zdot_follows_candidate_zdot(ref, C, n, seed):
+    x = _block(C, n, seed)
+    a = ref.ref_zdot(x)
+    b = ref.zdot(x)
+    scale = max(1.0, float(np.abs(a).max()))
+    assert float(np.abs(a - b).max()) <= 2e-5 * scale
+
+
+@pytest.mark.parametrize("td,fd,thr,nwidth,width,tbin", [(8, 4, 7.0, 2, 0.004, 0.001),
+                                                        (1, 1, 5.0, 1, 0.01, 0.001),
+                                                        (4, 1, 6.0, 3, 0.002, 0.0005),
+                                                        (2, 8, 4.0, 1, 0.0015, 0.00025)])
+@pytest.mark.parametrize("C,n,seed", [(64, 1000, 1), (128, 4096, 2), (40, 517, 3)])
+def test_kadaneF_equals_candidate_kadaneF(ref, C, n, seed, td, fd, thr, nwidth, width, tbin):
+    rng = np.random.default_rng(seed)
+    y = rng.normal(0.0, 1.0, (C, n)).astype(np.float32)
+    y[3, n // 5:n // 5 + n // 8] += 2.0                   # a long positive excursion
+    y[7, n // 20:n // 20 + 40] -= 3.0                     # a negative one
+    y[8:16, n // 2:n // 2 + 100] += 1.5                   # several channels at once
+    pre, want = ref.ref_kadaneF(y, td, fd, thr, nwidth, width, tbin)
+    # Candidate::kadaneF's limit (candidate.cpp:748): int(nwidth*width / tbin / td), the product
+    # in float, the divisions in double
+    wnlimit = int(float(np.float32(nwidth * np.float32(width))) / tbin / td)
+    got, ranges = ref.kadaneF(pre, td, fd, np.float32(thr) * np.float32(thr), wnlimit)
+    np.testing.assert_array_equal(got, want)
+    assert (ranges[:, ::2] >= 0).any(), "the planted excursions should be zapped"
+    assert not np.array_equal(want, pre)
