@@ -483,6 +483,9 @@ def ref_lib(variant="scalar") -> C.CDLL:
     L.ref_candidate_rfi.restype = C.c_int
     L.ref_candidate_rfi.argtypes = [f32p, C.c_int, C.c_long, C.c_double, C.c_float, C.c_int,
                                     C.c_int, C.c_int, C.c_float, C.c_int, C.c_void_p]
+    L.ref_candidate_downsample.restype = C.c_int
+    L.ref_candidate_downsample.argtypes = [f32p, C.c_int, C.c_long, C.c_void_p, C.c_int, C.c_int,
+                                           C.c_void_p, C.c_void_p]
     L.ref_cluster_run.restype = C.c_long
     L.ref_cluster_run.argtypes = [f32p, i32p, C.c_long, C.c_long, C.c_double, C.c_double,
                                   C.c_double, C.c_double, C.c_double, C.c_int, C.c_float,
@@ -538,6 +541,19 @@ def ref_kadaneF(x, td, fd, threshold, nwidth, width, tbin, variant="scalar"):
     ref_lib(variant).ref_candidate_rfi(x, x.shape[0], x.shape[1], tbin, width, 1, td, fd,
                                        threshold, nwidth, pre.ctypes.data)
     return pre, x
+
+
+def ref_downsample(x, freqs, td, fd, variant="scalar"):
+    """The reference's Candidate::downsample(td, fd) (candidate.cpp:381-427) on a [nchan][nbin]
+    block and its channel frequencies."""
+    x = np.ascontiguousarray(x, np.float32)
+    f = np.ascontiguousarray(freqs, np.float64)
+    nc, nb = x.shape[0] // fd, x.shape[1] // td
+    out = np.zeros((nc, nb), np.float32)
+    fout = np.zeros(nc, np.float64)
+    ref_lib(variant).ref_candidate_downsample(x, x.shape[0], x.shape[1], f.ctypes.data, td, fd,
+                                              out.ctypes.data, fout.ctypes.data)
+    return out, fout
 
 
 def ref_boxcar_run(tim, vwn, iqr=False, variant="scalar", nthreads=4):

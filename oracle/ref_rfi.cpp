@@ -8,7 +8,8 @@
  * op 1: get_stats + normalize (Candidate::kadaneF refuses unnormalised data,
  *       candidate.cpp:712-716), the normalised block copied to `normalized`, then
  *       kadaneF(td, fd, threshold, nwidth) with the candidate width `width` and bin `tbin`.
- * The block is overwritten with the result.
+ * The block is overwritten with the result.  ref_candidate_downsample runs
+ * Candidate::downsample(td, fd) (candidate.cpp:381-427) on a block and its frequencies.
  */
 #include <cstring>
 
@@ -38,5 +39,22 @@ extern "C" int ref_candidate_rfi(float *data, int nchan, long nbin, double tbin,
         return -1;
     }
     std::memcpy(data, c.data.data(), sizeof(float) * (size_t)nchan * nbin);
+    return 0;
+}
+
+extern "C" int ref_candidate_downsample(const float *data, int nchan, long nbin, const double *freqs,
+                                        int td, int fd, float *out, double *fout)
+{
+    num_threads = 1;
+    Candidate c;
+    c.npol = 1;
+    c.nchan = nchan;
+    c.nbin = nbin;
+    c.tbin = 1.;
+    c.frequencies.assign(freqs, freqs + nchan);
+    c.data.assign(data, data + (size_t)nchan * nbin);
+    c.downsample(td, fd);
+    std::memcpy(out, c.data.data(), sizeof(float) * (size_t)c.nchan * c.nbin);
+    std::memcpy(fout, c.frequencies.data(), sizeof(double) * (size_t)c.nchan);
     return 0;
 }

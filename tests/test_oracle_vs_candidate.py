@@ -1,8 +1,10 @@
-"""The oracle's main-path zdot and kadaneF (oracle/txoracle.c, the restatements the GPU kernels
-equal bit for bit) against the reference's own Candidate::zdot and Candidate::kadaneF
-(src/singlepulse/candidate.cpp:710-897, compiled in place with oracle/ref_rfi.cpp), the
-in-tree code the main path's XLibs RFI::zdot / RFI::kadaneF are restated from.  Both sides
-use the project's kadane<float> (oracle/refshim/utils.h: XLibs' version is not in the tree).
+"""The oracle's main-path zdot, kadaneF and downsample (oracle/txoracle.c, the restatements the
+GPU kernels equal bit for bit) against the reference's own Candidate::zdot, Candidate::kadaneF
+and Candidate::downsample (src/singlepulse/candidate.cpp:381-427, 710-897, compiled in place
+with oracle/ref_rfi.cpp), the in-tree code the main path's XLibs RFI::zdot / RFI::kadaneF /
+Downsample are restated from.  Both sides use the project's kadane<float>
+(oracle/refshim/utils.h: XLibs' version is not in the tree).  Downsample: bit-exact, samples
+and averaged frequencies.
 
 kadaneF: bit-exact on the normalised block Candidate::kadaneF sees, with the main path's
 squared threshold and the window limit Candidate computes.  zdot: the oracle folds its sums
@@ -56,3 +58,17 @@ def test_kadaneF_equals_candidate_kadaneF(ref, C, n, seed, td, fd, thr, nwidth, 
     np.testing.assert_array_equal(got, want)
     assert (ranges[:, ::2] >= 0).any(), "the planted excursions should be zapped"
     assert not np.array_equal(want, pre)
+
+
+@pytest.mark.parametrize("C,n0,td,fd", [(64, 1000, 1, 1), (64, 1000, 2, 1), (128, 4096, 4, 2),
+                                        (33, 517, 3, 4), (256, 2048, 16, 8)])
+def test_downsample_equals_candidate_downsample(ref, C, n0, td, fd):
+    """The unpack + sum-downsample of the oracle (time-major uint8 in, channel-major float out)
+    and its frequency averaging against Candidate::downsample on the same samples."""
+    rng = np.random.default_rng(C + n0 + td)
+    raw = np.clip(np.round(rng.normal(128, 20, (n0, C))), 0, 255).astype(np.uint8)
+    freqs = 1500.0 - np.arange(C) * 0.390625 + rng.uniform(-1e-3, 1e-3, C)
+    want, fwant = ref.ref_downsample(raw.T.astype(np.float32), freqs, td, fd)
+    got = ref.unpack_downsample(raw, td, fd)
+    np.testing.assert_array_equal(got, want)
+    np.testing.assert_array_equal(ref.downsample_freqs(freqs, fd), fwant)
