@@ -486,6 +486,8 @@ def ref_lib(variant="scalar") -> C.CDLL:
     L.ref_candidate_downsample.restype = C.c_int
     L.ref_candidate_downsample.argtypes = [f32p, C.c_int, C.c_long, C.c_void_p, C.c_int, C.c_int,
                                            C.c_void_p, C.c_void_p]
+    L.ref_dmdelay.restype = C.c_double
+    L.ref_dmdelay.argtypes = [C.c_double, C.c_double, C.c_double]
     L.ref_cluster_run.restype = C.c_long
     L.ref_cluster_run.argtypes = [f32p, i32p, C.c_long, C.c_long, C.c_double, C.c_double,
                                   C.c_double, C.c_double, C.c_double, C.c_int, C.c_float,

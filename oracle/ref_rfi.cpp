@@ -9,7 +9,8 @@
  *       candidate.cpp:712-716), the normalised block copied to `normalized`, then
  *       kadaneF(td, fd, threshold, nwidth) with the candidate width `width` and bin `tbin`.
  * The block is overwritten with the result.  ref_candidate_downsample runs
- * Candidate::downsample(td, fd) (candidate.cpp:381-427) on a block and its frequencies.
+ * Candidate::downsample(td, fd) (candidate.cpp:381-427) on a block and its frequencies;
+ * ref_dmdelay is Candidate::dmdelay (include/candidate.h:116-119).
  */
 #include <cstring>
 
@@ -58,3 +59,5 @@ extern "C" int ref_candidate_downsample(const float *data, int nchan, long nbin,
     std::memcpy(fout, c.frequencies.data(), sizeof(double) * (size_t)c.nchan);
     return 0;
 }
+
+extern "C" double ref_dmdelay(double dm, double fh, double fl) { return Candidate::dmdelay(dm, fh, fl); }

@@ -72,3 +72,15 @@ def test_downsample_equals_candidate_downsample(ref, C, n0, td, fd):
     got = ref.unpack_downsample(raw, td, fd)
     np.testing.assert_array_equal(got, want)
     np.testing.assert_array_equal(ref.downsample_freqs(freqs, fd), fwant)
+
+
+def test_dmdelay_equals_candidate_dmdelay(ref):
+    """The oracle's dispersion delay against Candidate::dmdelay, bit for bit (the product's
+    delay tables equal the oracle's, tests/test_host.py)."""
+    rng = np.random.default_rng(9)
+    L = ref.ref_lib("scalar")
+    for _ in range(200):
+        dm = float(rng.uniform(0, 5000))
+        fl, fh = sorted(rng.uniform(100, 3000, 2))
+        want = L.ref_dmdelay(dm, fh, fl)
+        assert ref.dmdelay(dm, fh, fl) == want
