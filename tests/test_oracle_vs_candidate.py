@@ -84,3 +84,14 @@ def test_dmdelay_equals_candidate_dmdelay(ref):
         fl, fh = sorted(rng.uniform(100, 3000, 2))
         want = L.ref_dmdelay(dm, fh, fl)
         assert ref.dmdelay(dm, fh, fl) == want
+
+
+def test_zdot_degenerate_blocks(ref):
+    """Constant channels (std 0 -> 1, candidate.cpp:850) everywhere make the zero-DM series 0
+    and the fit's determinant 0 (no fit, candidate.cpp:886); one channel makes the series the
+    channel itself."""
+    flat = np.tile(np.arange(8, dtype=np.float32)[:, None] * 3.0, (1, 100))
+    np.testing.assert_array_equal(ref.zdot(flat), ref.ref_zdot(flat))
+    one = np.random.default_rng(2).normal(0, 1, (1, 333)).astype(np.float32)
+    a, b = ref.ref_zdot(one), ref.zdot(one)
+    assert float(np.abs(a - b).max()) <= 2e-5 * max(1.0, float(np.abs(a).max()))
