@@ -65,3 +65,26 @@ def test_kernels_per_block_follow_run_block():
         assert bench.launches_per_block(sp, info, True, "fp16") == 16
     # the profiled 20-block command: 80 pushes, 194 gated row-blocks -> 3748 kernels
     assert 80 * bench.SKZAP_LAUNCHES + 240 * 13 + 194 * 2 == 3748
+
+
+def test_reference_arm_prints_its_line():
+    """`bench.py --impl reference` (the oracle port on the host cores, no GPU): one JSON line
+    with the contract's keys, the same metric as the GPU arm, zero host-device bytes."""
+    import json
+    import subprocess
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference",
+                        "--steps", "1", "--warmup", "0"], capture_output=True, text=True,
+                       timeout=600, cwd=root)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["metric"] == "DM-trial samples/s"
+    assert d["unit"] == d["metric"] and d["higher_is_better"] is True and d["value"] > 0
+    assert d["steps"] == 1 and d["warmup"] == 0 and d["n_gpus"] == 1
+    assert d["config"]["workload"] == "nchan4096_n2M_rfi_dm3000"
+    assert d["cpu_baseline"]["kind"] in ("port", "reference") and d["cpu_baseline"]["cores"] >= 1
+    assert d["cpu_baseline"]["value"] == d["value"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
