@@ -204,3 +204,16 @@ def test_stage1_delays_grow_with_the_group(tx, descending):
         assert (np.diff(d1, axis=0) >= 0).all(), (C, descending)
         np.testing.assert_array_equal(d1[-1], d1.max(axis=0))
         assert info.maxd1 == d1.max()
+
+
+def test_missing_library_fails_loudly(tx, tmp_path):
+    """Without the CUDA library the package refuses to run (ImportError naming the file and
+    that there is no CPU fallback); it never substitutes another implementation."""
+    missing = str(tmp_path / "libtxgpu.so")
+    saved = tx._lib
+    tx._lib = None
+    try:
+        with pytest.raises(ImportError, match="no CPU fallback"):
+            tx.load_library(missing)
+    finally:
+        tx._lib = saved
