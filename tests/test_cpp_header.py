@@ -81,6 +81,12 @@ def test_header_compiles_and_parses(tmp_path):
     vals = np.arange(12, dtype=np.float32) * np.float32(1.25) - np.float32(3.5)
     want = "".join("".join("%f " % v for v in vals[j * 4:(j + 1) * 4]) + "\n" for j in range(3))
     assert (tmp_path / "boxcar.txt").read_text() == want
+    # the Python mirror writes the same file
+    import transientx_gb300 as tx
+    tx.Boxcar(ndm=3, nsamples=4, mxS=vals.reshape(3, 4)).dump2txt(str(tmp_path / "py.txt"))
+    assert (tmp_path / "py.txt").read_text() == want
+    with pytest.raises(tx.TxgError):
+        tx.Boxcar(ndm=2, nsamples=2).dump2txt(str(tmp_path / "never.txt"))
     # without dense planes it refuses (TXG_ERR_STATE) instead of reading nothing
     assert "throws -6" in out
 

@@ -179,6 +179,34 @@ def _ptr(a: np.ndarray) -> int:
 # ---- configuration mirror --------------------------------------------------------------
 
 @dataclass
+class Boxcar:
+    """The public members of the reference's Boxcar (include/boxcar.h:31-43) for one (row,
+    beam) after its last block, as Search.boxcar fills them: mxS / mxwn are the dense
+    [ndm][nsamples] planes when the plan has FLAG_DENSE, else None; gated is what Boxcar::run
+    returned (boxcar.cpp:160-161)."""
+    counter: int = 0
+    tsamp: float = 0.0
+    nsamples: int = 0
+    dms: float = 0.0
+    ddm: float = 0.0
+    ndm: int = 0
+    maxwn: int = 0
+    fmin: float = 0.0
+    fmax: float = 0.0
+    mxS: Optional[np.ndarray] = None
+    mxwn: Optional[np.ndarray] = None
+    gated: bool = False
+
+    def dump2txt(self, fname: str) -> None:
+        """mxS as text, one line per DM trial, each value printed "%f " (boxcar.cpp:473-489)."""
+        if self.mxS is None:
+            raise TxgError(ERR_STATE, "dump2txt: no dense mxS (plan without FLAG_DENSE)")
+        with open(fname, "w") as f:
+            for row in np.asarray(self.mxS, np.float32).reshape(self.ndm, self.nsamples):
+                f.write("".join("%f " % v for v in row) + "\n")
+
+
+@dataclass
 class SinglePulse:
     """Configuration of one ddplan row, with the member names of the reference's SinglePulse
     (include/singlepulse.h:95-133) and its defaults (src/singlepulse/singlepulse.cpp:18-65,
@@ -425,6 +453,15 @@ class Search:
         pts = buf[:min(res.npoints, self.cap)].copy() if points else None
         cl = self._clbuf[:min(res.nclusters, len(self._clbuf))].copy()
         return res, pts, cl
+
+    def boxcar(self, row: int = 0, beam: int = 0) -> Boxcar:
+        """Boxcar's members for the row's last block; the dense planes with FLAG_DENSE."""
+        i = self.row_info(row, beam)
+        b = Boxcar(counter=i.counter, tsamp=i.tsamp, nsamples=i.nsamples, dms=i.dms, ddm=i.ddm,
+                   ndm=i.ndm, maxwn=i.maxwn, fmin=i.fmin, fmax=i.fmax, gated=bool(i.gated))
+        if self.flags & FLAG_DENSE:
+            b.mxS, b.mxwn = self.dense(row, beam)
+        return b
 
     def dense(self, row: int = 0, beam: int = 0) -> Tuple[np.ndarray, np.ndarray]:
         i = self.row_info(row, beam)
