@@ -153,6 +153,35 @@ def class_smem_bytes(info, elem, d1):
             8.0 * info.ndm * info.nsamples * info.nwidths]
 
 
+FP32_LANES_PER_SM = 128  # FP32 operations one SM issues per clock (4 partitions x 32 lanes)
+
+
+def class_fp32_ops(info):
+    """FP32 operations of one launch of the compute classes, one per lane instruction of the
+    algorithm: stage 1 one add per (channel, coarse DM, sample), stage 2 one add per (subband,
+    DM, output sample), the boxcar 3 per (DM, sample) for the statistics and running sum plus
+    4 per (DM, sample, width): subtract, multiply, compare, select.  Other classes: None."""
+    return [None, None, float(info.nchans) * info.ngroup * info.ndump,
+            float(info.nsub) * info.ndm * info.nsamples,
+            float(info.ndm) * info.nsamples * (3 + 4 * info.nwidths)]
+
+
+def alu_roofline(op_total, cls_ms, sm_mhz):
+    """FP32 operations per second of stage 1, stage 2 and the boxcar against 152 SMs x 128
+    lanes x the SM clock (one operation per lane per clock)."""
+    peak = NSM * FP32_LANES_PER_SM * float(sm_mhz) * 1e6 / 1e12
+    classes = {}
+    for c, name in ((2, "stage1"), (3, "stage2"), (4, "boxcar")):
+        if float(cls_ms[c]) > 0 and op_total[c]:
+            a = float(op_total[c]) / (float(cls_ms[c]) / 1e3) / 1e12
+            classes[name] = {"achieved": a, "frac": a / peak}
+    return {"unit": "Top/s", "peak": peak,
+            "peak_basis": f"{NSM} SMs x {FP32_LANES_PER_SM} FP32 lanes x median SM clock",
+            "basis": "stage 1 one add per (channel, coarse DM, sample), stage 2 one add per "
+                     "(subband, DM, sample), boxcar 3 per (DM, sample) + 4 per (DM, sample, "
+                     "width)", "classes": classes}
+
+
 def launches_per_block(sp, info, gated, precision="fp32"):
     """Kernels one block launches for one ddplan row (txg_api.cu run_block)."""
     n = 2  # unpack, equalize parameters
@@ -343,11 +372,14 @@ def run_ours(args, wl):
         for c in range(5):
             nb_total[c] += cb[c] * (tsteps * nblk if c < 3 else nblocks_r)
     sm_total = [0.0] * 5
+    op_total = [0.0] * 5
     for r, (sp, info) in enumerate(zip(wl.rows, infos)):
         d1 = tx.describe_row(wl.rows, r, fil.nchans, fil.tsamp, fil.freqs, wl.ndump)[1]
         sb = class_smem_bytes(info, ELEM[args.precision], d1)
+        ob = class_fp32_ops(info)
         for c in (2, 3, 4):
             sm_total[c] += sb[c] * (tsteps * nblk if c < 3 else tstats["gated"][r])
+            op_total[c] += ob[c] * (tsteps * nblk if c < 3 else tstats["gated"][r])
     peak, peak_kind = measured_peaks()
     achieved = nb_total[top] / (cls_ms[top] / 1e3) / 1e9
     roof = {"bound": "hbm", "kernel": names[top], "achieved": achieved, "peak": peak,
@@ -373,6 +405,8 @@ def run_ours(args, wl):
                                  "change within a thread set's coarse-DM groups (default shapes), "
                                  "stage 2 one per addition; two running-sum loads per sample and "
                                  "width (boxcar)"}
+
+    roof["alu"] = alu_roofline(op_total, cls_ms, (clk or {}).get("sm_mhz") or 2070.0)
 
     s.close()
     e2e = None

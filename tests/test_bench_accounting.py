@@ -88,3 +88,28 @@ def test_reference_arm_prints_its_line():
     assert d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}
+
+
+def test_alu_roofline_of_the_bench_workload():
+    """The FP32-operation roofline bench.py adds beside the HBM and shared-memory ones, on the
+    class times of a full FP32 bench (2 steps of 159 blocks, rows serialised): stage 1 adds at
+    a quarter of the 152 x 128 lanes x 2070 MHz peak; the line serialises to JSON."""
+    import json
+    import transientx_gb300 as tx
+    from transientx_gb300 import synth
+    wl = synth.WORKLOADS["nchan4096_n2M_rfi_dm3000"](nsamples=1 << 16)
+    cls_ms = np.array([67.3, 328.9, 904.7, 645.5, 431.1])
+    nblk, tsteps = 159, 2
+    op_total = [0.0] * 5
+    for r in range(len(wl.rows)):
+        info = tx.describe_row(wl.rows, r, wl.fil.nchans, wl.fil.tsamp, wl.fil.freqs, wl.ndump)[0]
+        ob = bench.class_fp32_ops(info)
+        for c in (2, 3, 4):
+            op_total[c] += ob[c] * tsteps * nblk
+    alu = bench.alu_roofline(op_total, cls_ms, 2070.0)
+    json.dumps(alu)
+    assert abs(alu["peak"] - 152 * 128 * 2.07e9 / 1e12) < 1e-9
+    assert set(alu["classes"]) == {"stage1", "stage2", "boxcar"}
+    assert 0.15 < alu["classes"]["stage1"]["frac"] < 0.35
+    for v in alu["classes"].values():
+        assert 0.0 < v["frac"] < 1.0
