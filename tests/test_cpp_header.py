@@ -96,3 +96,25 @@ def test_header_end_to_end(tmp_path):
     exe = _compile(tmp_path)
     r = subprocess.run([str(exe), "run"], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
+
+
+def test_integration_c_snippet_compiles(tmp_path):
+    """The C example of INTEGRATION.md section 2 compiles against the C header as written (its
+    free names, freqs and block, declared around it) and links with the library."""
+    import re
+    if not shutil.which("gcc"):
+        pytest.skip("no gcc")
+    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    blocks = re.findall(r"```c\n(.*?)```", doc, re.S)
+    assert blocks, "INTEGRATION.md has no C example"
+    body = blocks[0].replace('#include "transientx_gb300.h"', "")
+    src = tmp_path / "snippet.c"
+    src.write_text('#include <stdio.h>\n#include "transientx_gb300.h"\n'
+                   "int run(const double *freqs, const uint8_t *block) {\n" + body +
+                   "    return 0;\n}\nint main(void) { return 0; }\n")
+    from transientx_gb300 import _build
+    _build.build()
+    lib = os.path.join(ROOT, "transientx_gb300")
+    subprocess.run(["gcc", "-std=c11", "-Wall", "-Werror", "-Wno-unused-variable", str(src),
+                    "-I", os.path.join(ROOT, "include"), "-L", lib, "-ltxgpu",
+                    f"-Wl,-rpath,{lib}", "-o", str(tmp_path / "snippet")], check=True)
