@@ -118,3 +118,33 @@ def test_integration_c_snippet_compiles(tmp_path):
     subprocess.run(["gcc", "-std=c11", "-Wall", "-Werror", "-Wno-unused-variable", str(src),
                     "-I", os.path.join(ROOT, "include"), "-L", lib, "-ltxgpu",
                     f"-Wl,-rpath,{lib}", "-o", str(tmp_path / "snippet")], check=True)
+
+
+def test_integration_cpp_snippet_compiles(tmp_path):
+    """The C++ replacement of the block loop in INTEGRATION.md section 1 compiles against the
+    C++ layer as written, with the reference-side names it uses (the command-line map, the
+    reader, the writer and the output stream) declared around it."""
+    import re
+    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    blocks = [b for b in re.findall(r"```cpp\n(.*?)```", doc, re.S) if "transientx_gb300.hpp" in b]
+    assert len(blocks) == 1
+    body = blocks[0].replace('#include "transientx_gb300.hpp"', "")
+    prelude = r'''
+#include <fstream>
+#include <string>
+#include "transientx_gb300.hpp"
+struct OptionValue { float v; template <class T> T as() const { return (T)v; } };
+struct OptionMap { OptionValue operator[](const char *) const { return {4.f}; } };
+static bool read_raw_block(uint8_t *, long) { return false; }
+int run(const std::string &ddplan_text, const txgpu::SinglePulse &base_row, int nchans,
+        double tsamp, const std::vector<double> &frequencies, long ndump, const OptionMap &vm,
+        txgpu::CandsWriter &writer, std::ofstream &cands_file) {
+'''
+    src = tmp_path / "snippet.cpp"
+    src.write_text(prelude + body + "    return 0;\n}\nint main() { return 0; }\n")
+    from transientx_gb300 import _build
+    _build.build()
+    lib = os.path.join(ROOT, "transientx_gb300")
+    subprocess.run(["g++", "-std=c++17", "-Wall", "-Werror", "-Wno-unused-variable", str(src),
+                    "-I", os.path.join(ROOT, "include"), "-L", lib, "-ltxgpu",
+                    f"-Wl,-rpath,{lib}", "-o", str(tmp_path / "snippet")], check=True)
