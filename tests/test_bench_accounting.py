@@ -113,3 +113,21 @@ def test_alu_roofline_of_the_bench_workload():
     assert 0.15 < alu["classes"]["stage1"]["frac"] < 0.35
     for v in alu["classes"].values():
         assert 0.0 < v["frac"] < 1.0
+
+
+def test_profiled_stage1_traffic_matches_the_algorithmic_bytes():
+    """The DRAM traffic per stage-1 launch that bench.py reports (one ncu capture, mean over the
+    three rows' launches) is the algorithmic stage-1 bytes of those launches within 10 %:
+    each channel window crosses DRAM once and each subband sample is written once."""
+    import transientx_gb300 as tx
+    from transientx_gb300 import synth
+    wl = synth.WORKLOADS["nchan4096_n2M_rfi_dm3000"](nsamples=1 << 16)
+    for prec, elem in (("fp32", 4), ("fp16", 2)):
+        alg = []
+        for r, sp in enumerate(wl.rows):
+            info = tx.describe_row(wl.rows, r, wl.fil.nchans, wl.fil.tsamp, wl.fil.freqs,
+                                   wl.ndump)[0]
+            alg.append(bench.class_bytes(info, sp, wl.fil.nchans, wl.ndump, 0, elem)[2])
+        measured = bench.PROFILED_TRAFFIC[("nchan4096_n2M_rfi_dm3000", prec, "stage1")]
+        ratio = measured / (sum(alg) / len(alg))
+        assert 0.9 < ratio < 1.1, (prec, ratio)
