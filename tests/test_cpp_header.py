@@ -9,6 +9,8 @@ import pytest
 
 from conftest import ROOT
 
+GUIDE = os.path.join(ROOT, "INTEGRATION.md")  # the integration guide with the C and C++ examples
+
 SRC = r'''
 #include <cstdio>
 #include <cstdlib>
@@ -99,14 +101,15 @@ def test_header_end_to_end(tmp_path):
 
 
 def test_integration_c_snippet_compiles(tmp_path):
-    """The C example of INTEGRATION.md section 2 compiles against the C header as written (its
-    free names, freqs and block, declared around it) and links with the library."""
+    """The C example of the integration guide (section 2) compiles against the C header as
+    written (its free names, freqs and block, declared around it) and links with the
+    library."""
     import re
     if not shutil.which("gcc"):
         pytest.skip("no gcc")
-    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    doc = open(GUIDE).read()
     blocks = re.findall(r"```c\n(.*?)```", doc, re.S)
-    assert blocks, "INTEGRATION.md has no C example"
+    assert blocks, "the integration guide has no C example"
     body = blocks[0].replace('#include "transientx_gb300.h"', "")
     src = tmp_path / "snippet.c"
     src.write_text('#include <stdio.h>\n#include "transientx_gb300.h"\n'
@@ -121,11 +124,11 @@ def test_integration_c_snippet_compiles(tmp_path):
 
 
 def test_integration_cpp_snippet_compiles(tmp_path):
-    """The C++ replacement of the block loop in INTEGRATION.md section 1 compiles against the
-    C++ layer as written, with the reference-side names it uses (the command-line map, the
-    reader, the writer and the output stream) declared around it."""
+    """The C++ replacement of the block loop in the integration guide (section 1) compiles
+    against the C++ layer as written, with the reference-side names it uses (the command-line
+    map, the reader, the writer and the output stream) declared around it."""
     import re
-    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    doc = open(GUIDE).read()
     blocks = [b for b in re.findall(r"```cpp\n(.*?)```", doc, re.S) if "transientx_gb300.hpp" in b]
     assert len(blocks) == 1
     body = blocks[0].replace('#include "transientx_gb300.hpp"', "")
