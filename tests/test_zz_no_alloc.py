@@ -8,7 +8,25 @@ import ctypes
 import numpy as np
 import pytest
 
-pytestmark = pytest.mark.gpu
+# (ldx, nchans, nsamples, td, fd): inputs the entry point must refuse before queuing anything:
+# downsampled channels past the 65535 grid rows, fewer channels than fd, more samples than the
+# int32 zap ranges hold, and more downsampled samples than the fixed scratch
+BAD_ARGS = [
+    (16, 65536, 16, 8, 1),
+    (64, 3, 64, 8, 4),
+    (1 << 31, 1, 1 << 31, 1 << 11, 1),
+    (1 << 22, 4096, 1 << 22, 1, 1),
+]
+
+
+def test_kadane_noalloc_rejects_bad_sizes_before_touching_the_device(tx):
+    """The size checks return TXG_ERR_ARG before any CUDA call: they hold on a host without a
+    GPU, so on a GPU nothing can have been launched for these inputs."""
+    L = tx.load_library()
+    for ldx, C, N, td, fd in BAD_ARGS:
+        rc = L.txg_kadaneF_noalloc(ctypes.c_void_p(16), ldx, C, N, td, fd, 1.0, 1,
+                                   ctypes.c_void_p(16), None)
+        assert rc == tx.ERR_ARG, (ldx, C, N, td, fd)
 
 
 def _workload():
@@ -27,6 +45,7 @@ def _workload():
     return fil, plain, kad, ndump
 
 
+@pytest.mark.gpu
 def test_kadane_noalloc_matches_pipeline(tx):
     cudart = ctypes.CDLL("libcudart.so")
     L = tx.load_library()
@@ -66,9 +85,20 @@ def test_kadane_noalloc_matches_pipeline(tx):
                 np.testing.assert_array_equal(x_out, x_ref)
                 fired += int((r_ref[:, 0] >= 0).sum() + (r_ref[:, 2] >= 0).sum())
             assert fired > 0, "the sinusoid channels should trigger kadaneF"
-        # blocks beyond the fixed scratch are rejected, nothing is launched
-        rc = L.txg_kadaneF_noalloc(dx, 1 << 22, 4096, 1 << 22, 1, 1, thr2, wnlimit, dr, None)
-        assert rc == tx.ERR_ARG
+        # refused sizes (proved on the host by the test above) leave x and ranges untouched
+        x_keep = np.empty(C * ndump, np.float32)
+        r_keep = np.empty((C // fd) * 4, np.int32)
+        assert cudart.cudaMemcpy(x_keep.ctypes.data, dx, ctypes.c_size_t(nbytes), 2) == 0
+        assert cudart.cudaMemcpy(r_keep.ctypes.data, dr, ctypes.c_size_t(rbytes), 2) == 0
+        for ldx, nc, ns, tdb, fdb in BAD_ARGS:
+            rc = L.txg_kadaneF_noalloc(dx, ldx, nc, ns, tdb, fdb, thr2, wnlimit, dr, None)
+            assert rc == tx.ERR_ARG, (ldx, nc, ns, tdb, fdb)
+        assert cudart.cudaDeviceSynchronize() == 0
+        x_now, r_now = np.empty_like(x_keep), np.empty_like(r_keep)
+        assert cudart.cudaMemcpy(x_now.ctypes.data, dx, ctypes.c_size_t(nbytes), 2) == 0
+        assert cudart.cudaMemcpy(r_now.ctypes.data, dr, ctypes.c_size_t(rbytes), 2) == 0
+        np.testing.assert_array_equal(x_now, x_keep)
+        np.testing.assert_array_equal(r_now, r_keep)
     finally:
         cudart.cudaFree(dx)
         cudart.cudaFree(dr)

@@ -11,12 +11,16 @@
  * of the block that the maximum-sum scan reads) is the file-scope array below, reserved by
  * the loader on every GPU that loads the library and held until the process exits.
  *
- * Limit: (nsamples/td) * (nchans/fd) <= TXG_KADANE_NOALLOC_MAX floats (8 MiB); larger blocks
- * are rejected with TXG_ERR_ARG.  All calls share the array and each call overwrites every
+ * Limits: (nsamples/td) * (nchans/fd) <= TXG_KADANE_NOALLOC_MAX floats (8 MiB), nchans/fd
+ * between 1 and 65535 (one grid row per downsampled channel) and nsamples <= 2^31 - 1 (the
+ * zapped windows are int32 sample indices); anything else is rejected with TXG_ERR_ARG
+ * before any kernel is queued, so x and ranges stay untouched.  All calls share the array and each call overwrites every
  * element it reads before reading it, so nothing has to start at zero; calls whose work
  * overlaps on the GPU (for example on two streams at once) race on it.  The first call on a
  * device looks up the array's device address (cudaGetSymbolAddress) with that device
- * current; make that first call before any stream capture on the device.
+ * current; make that first call before any stream capture on the device.  The address is
+ * kept for the life of the process: a caller that destroys the device's primary context
+ * (cudaDeviceReset) must not call this entry point on that device afterwards.
  */
 #include <mutex>
 
@@ -39,6 +43,10 @@ extern "C" int txg_kadaneF_noalloc(float *x, int64_t ldx, int32_t nchans, int64_
     if (!x || !ranges || nchans < 1 || nsamples < 1 || td < 1 || fd < 1 || ldx < nsamples)
         return txg::set_arg_error("txg_kadaneF_noalloc: need x, ranges, nchans >= 1, "
                                   "nsamples >= 1, td, fd >= 1, ldx >= nsamples");
+    if (nchans < fd || nchans / fd > 65535)
+        return txg::set_arg_error("txg_kadaneF_noalloc: nchans/fd must be between 1 and 65535");
+    if (nsamples > 0x7fffffffLL)
+        return txg::set_arg_error("txg_kadaneF_noalloc: nsamples must fit the int32 zap ranges");
     const long long need = (long long)(nsamples / td) * (long long)(nchans / fd);
     if (need > TXG_KADANE_NOALLOC_MAX)
         return txg::set_arg_error("txg_kadaneF_noalloc: (nsamples/td)*(nchans/fd) = " +
