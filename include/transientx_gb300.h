@@ -225,7 +225,6 @@ int txg_get_tables(txg_handle *h, int32_t row, int32_t *d1, int32_t *d2, int32_t
 int txg_describe_row(const txg_plan *plan, int32_t row, txg_row_info *info, int32_t *d1,
                      int32_t *d2, int32_t *sub_start, int32_t *vwn);
 
-/* Boxcar width ladder of SinglePulse::prepare (singlepulse.cpp:242-254); returns the count. */
 /* Self-test of the failure path of every kernel that waits for its shared-memory copies: one
  * CTA waits, with the same bounded wait, for a 256-byte bulk copy.  never_complete = 0: the copy
  * completes (TXG_OK).  never_complete != 0: its barrier expects more bytes than the copy brings,
@@ -234,6 +233,7 @@ int txg_describe_row(const txg_plan *plan, int32_t row, txg_row_info *info, int3
  * No reference counterpart. */
 int txg_selftest_wait(int32_t never_complete, int32_t limit_ms);
 
+/* Boxcar width ladder of SinglePulse::prepare (singlepulse.cpp:242-254); returns the count. */
 int txg_width_ladder(float minw, float maxw, float snrloss, double tsamp, int32_t *vwn,
                      int32_t cap);
 
@@ -258,9 +258,11 @@ int txg_cluster(const txg_cand *cands, int64_t n, double dms, double ddm, double
  * to 0 in place; ranges: device output [nchans/fd][4] as in txg_get_zap_ranges; thr2: squared
  * S/N threshold; wnlimit: minimum window in downsampled samples; stream: cudaStream_t or
  * NULL.  Its scratch is a fixed device array of 2^21 floats (8 MiB) that every GPU loading the
- * library holds until exit: (nsamples/td)*(nchans/fd) above that returns TXG_ERR_ARG.  Calls
+ * library holds until exit: (nsamples/td)*(nchans/fd) above that returns TXG_ERR_ARG, and so
+ * do nchans/fd outside 1..65535 and nsamples above 2^31-1, before anything is queued.  Calls
  * share that array, so calls overlapping on the GPU race.  The first call on a device looks up
- * the array's address; make it before any stream capture on that device. */
+ * the array's address; make it before any stream capture on that device, and make no call on
+ * a device after cudaDeviceReset there (the address kept from the first call is stale). */
 int txg_kadaneF_noalloc(float *x, int64_t ldx, int32_t nchans, int64_t nsamples, int32_t td,
                         int32_t fd, float thr2, int64_t wnlimit, int32_t *ranges, void *stream);
 

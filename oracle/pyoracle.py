@@ -13,7 +13,10 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_TREE = "/root/reference"
+# the TransientX source tree whose boxcar.cpp, cluster.cpp and candidate.cpp are compiled in
+# place (read-only); TXREF_TREE overrides the checkout's usual mount point.  Where no tree
+# exists (a machine without the reference) only the oracle itself is built.
+REF_TREE = os.environ.get("TXREF_TREE", "/root/reference")
 
 f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")

@@ -49,12 +49,16 @@ def assert_boxcar_close(tim, vwn, S_gpu, W_gpu, S_ref, W_ref, rel=REL, iqr=False
 
 
 def assert_cands_close(c_gpu, c_ref, thre, rel=REL):
-    """Same (idm, isamp) sets except points within rel of the threshold."""
+    """Same (idm, isamp) sets except points whose S lies within rel (relative) of the
+    threshold in either list; S of the common points within rel*max(1,|S|)."""
     a = {(int(x["idm"]), int(x["isamp"])): float(x["S"]) for x in c_gpu}
     b = {(int(x["idm"]), int(x["isamp"])): float(x["S"]) for x in c_ref}
+    band = rel * max(1.0, thre)
     for k in set(a) ^ set(b):
         s = a.get(k, b.get(k))
-        assert abs(s - thre) <= rel * max(1.0, thre) * 2, f"point {k} S={s} not near threshold"
+        assert abs(s - thre) <= band, f"point {k} S={s} not within {rel} of the threshold"
+    for k in set(a) & set(b):
+        assert abs(a[k] - b[k]) <= rel * max(1.0, abs(b[k])), f"point {k}: S {a[k]} vs {b[k]}"
     # the reported order is row-major (Cluster::run scan order)
     keys = [(int(x["idm"]), int(x["isamp"])) for x in c_gpu]
     assert keys == sorted(keys)
