@@ -136,6 +136,17 @@ void txg_destroy(txg_handle *h);
 int txg_push_block(txg_handle *h, int32_t beam, const uint8_t *host, int64_t nsamp);
 int txg_push_block_device(txg_handle *h, int32_t beam, const uint8_t *dev, int64_t nsamp);
 
+/* Start a new observation on a beam: the next block pushed to it is the first block of a new
+ * file, its history, sample counter and subband rings as at txg_create.  Blocks queued
+ * before the call are searched as part of the previous observation and their results are
+ * popped in push order as usual (txg_pop_result; row info and the inspection calls describe
+ * the newest harvested block).  Nothing waits on the host: the beam's buffers are cleared on
+ * the device after its queued blocks.  The reference prepares a fresh SinglePulse for every
+ * observation it searches (dedisperse_fil.cpp:292-311, SinglePulse::prepare,
+ * singlepulse.cpp:206-254); a handle reused for file after file calls this instead of
+ * txg_destroy + txg_create.  Cost: one device memset of the beam's rings. */
+int txg_reset_beam(txg_handle *h, int32_t beam);
+
 /* Wait for queued work and collect candidates; returns TXG_ERR_OVERFLOW if any buffer
  * overflowed since the last call. */
 int txg_sync(txg_handle *h);

@@ -206,6 +206,58 @@ def dmdelay(dm, fh, fl):
     return lib().txo_dmdelay(dm, fh, fl)
 
 
+# ---- subband plan: the oracle's own choice of subband count and DM group -------------------
+# The reference leaves both to XLibs' SubbandDedispersion; this rule defines them for the
+# oracle and for the CPU baseline, which must not take its plan from the product library.
+
+def _subband_edges(freqs, nsub):
+    """First channel of each subband (channels j with j*nsub/C = s) and the highest and lowest
+    frequency of each."""
+    C_ = len(freqs)
+    start = [(s * C_ + nsub - 1) // nsub for s in range(nsub + 1)]
+    fref = [max(freqs[start[s]:start[s + 1]]) for s in range(nsub)]
+    flow = [min(freqs[start[s]:start[s + 1]]) for s in range(nsub)]
+    return start, fref, flow
+
+
+def plan_group(freqs, nsub, tsamp, ddm, ndm):
+    """Largest DM group whose smearing within a subband stays within one sample:
+    group*ddm/2 * max_s dmdelay(1, fref_s, flow_s) <= tsamp, rounded down to a multiple of 8
+    when at least 8, between 1 and ndm."""
+    _, fref, flow = _subband_edges(freqs, nsub)
+    kmax = max(dmdelay(1.0, h, l) for h, l in zip(fref, flow))
+    if not ddm * kmax > 0.0:
+        return int(min(max(ndm, 1), 1 << 30))
+    g = np.floor(2.0 * tsamp / (ddm * kmax))
+    if g >= 8.0:
+        g = np.floor(g / 8.0) * 8.0
+    return int(min(max(g, 1.0), float(ndm)))
+
+
+def plan_nsub(freqs, tsamp, ddm, ndm):
+    """The power of two (<= C) minimising the additions per output sample,
+    C*ceil(ndm/group) + nsub*ndm; ties go to the smaller count."""
+    C_ = len(freqs)
+    best, bestcost, p = 1, None, 1
+    while p <= C_:
+        g = plan_group(freqs, p, tsamp, ddm, ndm)
+        cost = float(C_) * float((ndm + g - 1) // g) + float(p) * float(ndm)
+        if bestcost is None or cost < bestcost:
+            best, bestcost = p, cost
+        p *= 2
+    return best
+
+
+def plan_row(freqs_raw, tsamp_raw, td, fd, ddm, ndm, nsub=0, group=0):
+    """(nsub, group) of one ddplan row on the td x fd downsampled channels: the given values
+    where positive, else the rule above."""
+    f = downsample_freqs(np.asarray(freqs_raw, np.float64), fd)
+    tsamp = tsamp_raw * td
+    ns = min(nsub, len(f)) if nsub > 0 else plan_nsub(f, tsamp, ddm, ndm)
+    g = min(group, ndm) if group > 0 else plan_group(f, ns, tsamp, ddm, ndm)
+    return ns, g
+
+
 def width_ladder(minw, maxw, snrloss, tsamp, cap=256):
     out = np.zeros(cap, np.int32)
     n = lib().txo_width_ladder(minw, maxw, snrloss, tsamp, out, cap)

@@ -67,15 +67,21 @@ def test_kernels_per_block_follow_run_block():
     assert 80 * bench.SKZAP_LAUNCHES + 240 * 13 + 194 * 2 == 3748
 
 
-def test_reference_arm_prints_its_line():
+@pytest.mark.parametrize("workload", ["beams64_nchan1024_4096", "nchan4096_n2M_rfi_dm3000"])
+def test_reference_arm_prints_its_line(workload):
     """`bench.py --impl reference` (the oracle port on the host cores, no GPU): one JSON line
-    with the contract's keys, the same metric as the GPU arm, zero host-device bytes."""
+    with the contract's keys, the same metric as the GPU arm, zero host-device bytes; it
+    plans with the oracle's own rule and never loads the product library."""
     import json
     import subprocess
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference",
-                        "--steps", "1", "--warmup", "0"], capture_output=True, text=True,
-                       timeout=600, cwd=root)
+    probe = ("import runpy, sys; sys.argv = ['bench.py'] + sys.argv[1:]; "
+             "runpy.run_path('bench.py', run_name='__main__'); "
+             "maps = open('/proc/self/maps').read(); "
+             "assert 'libtxgpu' not in maps, 'the reference arm loaded the product library'")
+    r = subprocess.run([sys.executable, "-c", probe, "--impl", "reference", "--workload",
+                        workload, "--steps", "1", "--warmup", "0"], capture_output=True,
+                       text=True, timeout=900, cwd=root)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
     assert len(lines) == 1
@@ -83,7 +89,7 @@ def test_reference_arm_prints_its_line():
     assert d["impl"] == "reference" and d["metric"] == "DM-trial samples/s"
     assert d["unit"] == d["metric"] and d["higher_is_better"] is True and d["value"] > 0
     assert d["steps"] == 1 and d["warmup"] == 0 and d["n_gpus"] == 1
-    assert d["config"]["workload"] == "nchan4096_n2M_rfi_dm3000"
+    assert d["config"]["workload"] == workload
     assert d["cpu_baseline"]["kind"] in ("port", "reference") and d["cpu_baseline"]["cores"] >= 1
     assert d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
@@ -128,6 +134,54 @@ def test_profiled_stage1_traffic_matches_the_algorithmic_bytes():
             info = tx.describe_row(wl.rows, r, wl.fil.nchans, wl.fil.tsamp, wl.fil.freqs,
                                    wl.ndump)[0]
             alg.append(bench.class_bytes(info, sp, wl.fil.nchans, wl.ndump, 0, elem)[2])
-        measured = bench.PROFILED_TRAFFIC[("nchan4096_n2M_rfi_dm3000", prec, "stage1")]
+        measured = bench.profiled_traffic("nchan4096_n2M_rfi_dm3000", prec, "stage1")[0]
         ratio = measured / (sum(alg) / len(alg))
         assert 0.9 < ratio < 1.1, (prec, ratio)
+
+
+def test_lane_schedule_walks_every_beam_in_order():
+    """Lanes of one channel count take that count's beams in job order, push each beam's
+    blocks from 0 consecutively and reset exactly when they change beam; the job's beams are
+    all started, in order, before any starts again."""
+    from transientx_gb300 import synth
+    job = synth.beams64()
+    ids = list(range(len(job.beams)))
+    lanes, bps = 3, 2
+    per_chan = max(sum(job.nblocks(b) for b in ids if job.beams[b].nchans == C)
+                   for C in (1024, 4096))
+    nsteps = (3 * per_chan) // (2 * lanes * bps)  # about one and a half passes over the job
+    chans, steps = bench.lane_schedule(job, ids, lanes, nsteps, bps)
+    assert chans == [1024, 4096]
+    for C in chans:
+        order = [b for b in ids if job.beams[b].nchans == C]
+        starts, prev = [], {}
+        for st in steps:
+            for c, lane, b, k, reset in st:
+                if c != C:
+                    continue
+                assert job.beams[b].nchans == C and k < job.nblocks(b)
+                p = prev.get(lane)
+                if p is None or p[0] != b or k == 0:
+                    assert k == 0 and reset == (p is not None), (lane, b, k, p)
+                    starts.append(b)
+                else:
+                    assert k == p[1] + 1 and not reset
+                prev[lane] = (b, k)
+        assert len(starts) > len(order), "the schedule should run through the job"
+        assert starts == (order * (len(starts) // len(order) + 1))[:len(starts)]
+
+
+def test_pipeline_bytes_of_the_rfi_workload():
+    """The pipeline roofline's algorithmic bytes per block of the 4096-channel workload (FP32):
+    the raw block three times (RFI filters on) plus each row's subband series written and read
+    once: 7.3 GB per block, halved series in 16-bit storage."""
+    import transientx_gb300 as tx
+    from transientx_gb300 import synth
+    wl = synth.WORKLOADS["nchan4096_n2M_rfi_dm3000"](nsamples=1 << 16)
+    infos = [tx.describe_row(wl.rows, r, wl.fil.nchans, wl.fil.tsamp, wl.fil.freqs, wl.ndump)[0]
+             for r in range(len(wl.rows))]
+    raw = 4096 * wl.ndump
+    series = sum(2 * i.nsub * i.ngroup * i.ndump for i in infos)
+    assert bench.b_alg_block(infos, wl.rows, 4096, wl.ndump, 4, 10) == 3 * raw + 4 * series + 160
+    assert bench.b_alg_block(infos, wl.rows, 4096, wl.ndump, 2, 0) == 3 * raw + 2 * series
+    assert 7.1e9 < bench.b_alg_block(infos, wl.rows, 4096, wl.ndump, 4, 0) < 7.5e9

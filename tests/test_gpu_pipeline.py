@@ -469,3 +469,54 @@ def test_streamed_blocks_equal_synced_blocks(tx, prec, pinned, nbeams):
                 np.testing.assert_array_equal(u[3], v[3], err_msg=where + " clusters")
                 npts += len(u[2])
     assert npts > 0, "the injected pulses should give points above threshold"
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp16"])
+def test_reset_beam_equals_fresh_handle(tx, prec):
+    """A beam that searched one file and is reset (txg_reset_beam) gives, block for block, the
+    series, points and clusters that a fresh handle gives for the next file, while the other
+    beam of the handle is unaffected; the first file's last results stay poppable."""
+    from transientx_gb300 import synth
+    fil, rows, ndump = small_workload()
+    other = synth.Filterbank(fil.nchans, fil.tsamp, fil.freqs, fil.nsamples, 77,
+                             pulses=[(0.6 * fil.nsamples * fil.tsamp, 120.0, 2e-3, 25.0)])
+    nblk = fil.nsamples // ndump
+    flags = tx.FLAG_KEEP_SERIES
+    with tx.Search(rows, fil.nchans, fil.tsamp, fil.freqs, ndump, nbeams=2, precision=prec,
+                   flags=flags) as s, \
+            tx.Search(rows, fil.nchans, fil.tsamp, fil.freqs, ndump, precision=prec,
+                      flags=flags) as fresh:
+        for b in range(3):  # a first, partial file on beam 0
+            s.push_block(fil.generate(b * ndump, ndump), beam=0)
+        s.reset_beam(0)
+        first = True
+        ngated = 0
+        for b in range(nblk):
+            raw = other.generate(b * ndump, ndump)
+            s.push_block(raw, beam=0)
+            s.push_block(raw, beam=1)
+            fresh.push_block(raw)
+            s.sync()
+            fresh.sync()
+            if first:  # the first file's three blocks, then the new file's first block
+                for r in range(len(rows)):
+                    counters = []
+                    while True:
+                        out = s.pop_result(r, beam=0, points=False)
+                        if out is None:
+                            break
+                        counters.append(out[0].counter)
+                    N = s.row_info(r).ndump
+                    assert counters == [N, 2 * N, 3 * N, N], counters
+                first = False
+            for r in range(len(rows)):
+                a, f = s.row_info(r, beam=0), fresh.row_info(r)
+                assert (a.counter, a.gated) == (f.counter, f.gated)
+                if not f.gated:
+                    continue
+                ngated += 1
+                np.testing.assert_array_equal(s.timdata(r, beam=0), fresh.timdata(r))
+                np.testing.assert_array_equal(s.candidates(r, beam=0), fresh.candidates(r))
+                np.testing.assert_array_equal(s.candidates(r, beam=1), fresh.candidates(r))
+                np.testing.assert_array_equal(s.cluster(r, beam=0), fresh.cluster(r))
+        assert ngated >= 4

@@ -217,3 +217,22 @@ def test_missing_library_fails_loudly(tx, tmp_path):
             tx.load_library(missing)
     finally:
         tx._lib = saved
+
+
+def test_oracle_planner_equals_host_planner(tx, oracle):
+    """The oracle's own subband plan (what the CPU baseline uses without the product library)
+    gives the nsub and DM group that the library's host planner picks, on every benchmarked
+    row and on both channel counts of the many-beam workload."""
+    from transientx_gb300 import synth
+    cases = []
+    for name in ("nchan256_n1M_dm1000", "nchan4096_n2M_rfi_dm3000", "nchan8192_n8M_dm5000"):
+        wl = synth.WORKLOADS[name](nsamples=1 << 16)
+        cases.append((wl.rows, wl.fil.nchans, wl.fil.tsamp, wl.fil.freqs, wl.ndump))
+    wl = synth.WORKLOADS["nchan4096_n2M_rfi_dm3000"](nsamples=1 << 16)
+    for C in (1024, 2048):
+        cases.append((wl.rows, C, wl.fil.tsamp, synth.band(C, 1712.0, 856.0), wl.ndump))
+    for rows, C, tsamp, f, ndump in cases:
+        for r, sp in enumerate(rows):
+            info = tx.describe_row(rows, r, C, tsamp, f, ndump)[0]
+            assert oracle.plan_row(f, tsamp, sp.td, sp.fd, sp.ddm, sp.ndm, sp.nsub,
+                                   sp.dm_group) == (info.nsub, info.dm_group), (C, r)

@@ -106,7 +106,7 @@ EXPORTS = [
     "txg_cluster", "txg_get_timing", "txg_get_stream", "txg_strerror", "txg_version",
     "txg_describe_row", "txg_pop_result", "txg_get_mask", "txg_kadaneF_noalloc",
     "txg_get_subdata", "txg_cand_band", "txg_replot", "txg_get_timdata_q", "txg_result_ready",
-    "txg_selftest_wait",
+    "txg_selftest_wait", "txg_reset_beam",
 ]
 
 _lib: Optional[C.CDLL] = None
@@ -131,6 +131,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.txg_push_block.argtypes = [vp, C.c_int32, vp, C.c_int64]
     L.txg_push_block_device.argtypes = [vp, C.c_int32, vp, C.c_int64]
     L.txg_sync.argtypes = [vp]
+    L.txg_reset_beam.argtypes = [vp, C.c_int32]
     L.txg_get_row_info.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(txg_row_info)]
     L.txg_get_candidates.argtypes = [vp, C.c_int32, C.c_int32, vp, C.c_int64,
                                      C.POINTER(C.c_int64)]
@@ -407,6 +408,11 @@ class Search:
             return rc
         _check(rc, "txg_sync")
         return rc
+
+    def reset_beam(self, beam: int = 0) -> None:
+        """Begin a new observation on `beam` (txg_reset_beam): the next block pushed is the
+        first of a new file; blocks queued before belong to the previous one."""
+        _check(load_library().txg_reset_beam(self.h, beam), "reset_beam")
 
     def row_info(self, row: int = 0, beam: int = 0) -> txg_row_info:
         info = txg_row_info()

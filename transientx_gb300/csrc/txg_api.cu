@@ -1000,6 +1000,29 @@ int txg_sync(txg_handle *h)
     return status;
 }
 
+int txg_reset_beam(txg_handle *h, int32_t beam)
+{
+    DeviceScope device_scope(h);
+    if (!h) return fail(TXG_ERR_ARG, "null handle");
+    if (beam < 0 || beam >= (int)h->br.size()) return fail(TXG_ERR_ARG, "beam out of range");
+    const bool timing = h->flags & TXG_FLAG_TIMING;
+    /* history columns and subband rings back to their state at txg_create (zeros), ordered on
+     * each row's stream after the beam's queued blocks and before its next one; nothing waits
+     * on the host.  The slots keep rotating, so blocks queued before the reset are harvested
+     * and popped in push order as usual. */
+    for (size_t r = 0; r < h->br[beam].size(); r++) {
+        const RowPlan &P = h->rp[r];
+        BeamRow &b = h->br[beam][r];
+        const cudaStream_t rs = timing ? h->st : h->rst[r];
+        for (int i = 0; i < 2; i++)
+            if (b.xh[i]) TXG_CUDA_TRY(cudaMemsetAsync(b.xh[i], 0, sizeof(float) * P.C * P.ldh, rs));
+        if (b.x16) TXG_CUDA_TRY(cudaMemsetAsync(b.x16, 0, sizeof(__half) * P.C * P.ldh, rs));
+        TXG_CUDA_TRY(cudaMemsetAsync(b.ring, 0, (size_t)P.ng * P.nsub * P.R * ring_elem(h->prec), rs));
+        b.pushed = 0;
+    }
+    return TXG_OK;
+}
+
 int txg_get_row_info(txg_handle *h, int32_t beam, int32_t row, txg_row_info *out)
 {
     int rc = check_beam_row(h, beam, row);

@@ -177,6 +177,44 @@ def nchan8192_dm5000(seed: int = 5, nsamples: int = 1 << 23) -> Workload:
     return Workload("nchan8192_n8M_dm5000", fil, rows, seglen_ndump(tsamp, [1, 2, 4, 8, 16]))
 
 
+@dataclass
+class BeamJob:
+    """Many independent beams searched with one ddplan: the beams differ in length and channel
+    count; every beam has its own seeded filterbank."""
+    name: str
+    beams: List[Filterbank]
+    rows: List[SinglePulse]
+    ndump: int
+
+    def nblocks(self, b: int) -> int:
+        return self.beams[b].nsamples // self.ndump
+
+
+def beams64(seed: int = 4, nbeams: int = 64) -> BeamJob:
+    """64 beams of uneven length: 2^U(19,22) samples (log-uniform, seeded), 1024 or 4096
+    channels (seeded coin) over 856-1712 MHz at 76 us, uint8 Gaussian noise (mean 128, sigma
+    12) with 0-5 injected pulses per beam (DM 20-3000, width 0.1-30 ms log-uniform, S/N 8-50).
+    Beam b uses seed + b.  The ddplan is the 4096-channel workload's (three rows to DM 3000
+    with td 1/2/4, rfilist kadaneF 8 4, zdot), so both channel counts share the block length
+    (13156 samples, 1 s)."""
+    rng = np.random.default_rng(seed)
+    tsamp = 76e-6
+    lens = np.round(2.0 ** rng.uniform(19.0, 22.0, nbeams)).astype(np.int64)
+    chans = np.where(rng.random(nbeams) < 0.5, 1024, 4096)
+    beams = []
+    for b in range(nbeams):
+        T = float(lens[b]) * tsamp
+        k = int(rng.integers(0, 6))
+        pulses = [(float(t0), float(dm), float(w), float(sn)) for t0, dm, w, sn in zip(
+            np.sort(rng.uniform(0.05 * T, 0.9 * T, k)), rng.uniform(20.0, 3000.0, k),
+            np.exp(rng.uniform(np.log(1e-4), np.log(3e-2), k)), rng.uniform(8.0, 50.0, k))]
+        C_ = int(chans[b])
+        beams.append(Filterbank(C_, tsamp, band(C_, 1712.0, 856.0), int(lens[b]), seed + b,
+                                pulses=pulses))
+    rows = nchan4096_rfi(nsamples=1 << 16).rows
+    return BeamJob("beams64_nchan1024_4096", beams, rows, seglen_ndump(tsamp, [1, 2, 4]))
+
+
 def replot_candidates(n: int, nchan: int = 4096, seed: int = 9, dm: float = 500.0,
                       width: float = 2e-3, tbin: float = 76e-6, nwidth: int = 20):
     """Candidates as replot_fil cuts them (replot_fil.cpp:300-306): nbin = (delay across the
@@ -201,3 +239,5 @@ def replot_candidates(n: int, nchan: int = 4096, seed: int = 9, dm: float = 500.
 
 WORKLOADS = {"nchan256_n1M_dm1000": nchan256_single, "nchan4096_n2M_rfi_dm3000": nchan4096_rfi,
              "nchan8192_n8M_dm5000": nchan8192_dm5000}
+# workloads of many beams (BeamJob)
+JOBS = {"beams64_nchan1024_4096": beams64}
