@@ -71,7 +71,7 @@ def parse_args():
     return a
 
 
-JOBS_NAMES = ("beams64_nchan1024_4096",)
+JOBS_NAMES = ("beams64_nchan1024_4096", "beams16_nchan8192_dm5000")
 
 
 # ---- clocks during the timed region -------------------------------------------------------
@@ -128,16 +128,13 @@ def measured_peaks():
 # ---- algorithmic bytes per kernel class (per launch, per row) ----------------------------
 def class_bytes(info, sp, nchans_raw, ndump_raw, ncand, elem):
     """Bytes a perfect implementation must move for one launch of each class:
-    unpack: raw uint8 in + float block out; preprocess: read+write the block once (16-bit
-    precisions: plus its FP16 copy out); stage 1: block in (FP32, or its FP16 copy) + subband
-    series out; stage 2: subband series in + dedispersed out; boxcar: dedispersed series in +
-    16-byte candidates out."""
+    unpack: raw uint8 in + float block out; preprocess: read+write the block once; stage 1:
+    the FP32 block in + subband series out (elem bytes per element); stage 2: subband series
+    in + dedispersed out; boxcar: dedispersed series in + 16-byte candidates out."""
     C, N = info.nchans, info.ndump
     block = 4.0 * C * N
-    block_in = float(elem) * C * N
     series = float(elem) * info.nsub * info.ngroup * N
-    pre = 2 * block + (block_in if elem == 2 else 0.0)
-    return [nchans_raw * ndump_raw + block, pre, block_in + series,
+    return [nchans_raw * ndump_raw + block, 2 * block, block + series,
             series + 4.0 * info.ndm * info.nsamples, 4.0 * info.ndm * info.nsamples + 16 * ncand]
 
 
@@ -166,11 +163,11 @@ def stage1_window_loads(d1):
 
 def class_smem_bytes(info, elem, d1):
     """Shared-memory bytes one launch of the classes bound by shared memory loads: stage 1 one
-    window element per sample for each delay change within a thread set's groups (the loads
-    the kernel makes; additions are C x ngroup x N), stage 2 one window element per addition
-    (nsub x ndm x (N + noverlap)), the boxcar two running-sum values per (sample, width).
-    Other classes: None."""
-    return [None, None, float(elem) * info.ndump * stage1_window_loads(d1),
+    FP32 window element per sample for each delay change within a thread set's groups (the
+    loads the kernel makes; additions are C x ngroup x N), stage 2 one ring element (elem
+    bytes) per addition (nsub x ndm x (N + noverlap)), the boxcar two running-sum values per
+    (sample, width).  Other classes: None."""
+    return [None, None, 4.0 * info.ndump * stage1_window_loads(d1),
             float(elem) * info.nsub * info.ndm * info.nsamples,
             8.0 * info.ndm * info.nsamples * info.nwidths]
 
@@ -212,8 +209,6 @@ def launches_per_block(sp, info, gated, precision="fp32"):
         n += 1
     for op in sp.rfilist:
         n += RFI_LAUNCHES[op[0]]
-    if precision != "fp32":
-        n += 1  # FP16 copy of the block
     n += 1  # stage 1
     if gated:
         n += 1 + (2 if info.nsamples > BOXCAR_ROW_MAX else 1)  # stage 2, boxcar
@@ -371,11 +366,13 @@ def run_single(args, wl):
 
     def make_search(flags):
         return tx.Search(wl.rows, fil.nchans, fil.tsamp, fil.freqs, wl.ndump,
-                         precision=args.precision, flags=flags, zapthre=ZAPTHRE)
+                         precision=args.precision, flags=flags | tx.FLAG_AUTOTUNE,
+                         zapthre=ZAPTHRE)
 
     # the headline pass: the rows of a block run concurrently, each on its own stream
     s = make_search(0)
     infos = [s.row_info(r) for r in range(len(wl.rows))]
+    shapes = [list(s.launch_shape(r)) for r in range(len(wl.rows))]
     stream = torch.cuda.ExternalStream(s.stream())
 
     def drain(stats):
@@ -500,8 +497,7 @@ def run_single(args, wl):
     if not args.no_e2e:
         # the public host-pointer path: pinned host blocks, H2D inside the timed region, and
         # Cluster::run on every block inside the library while the device runs ahead
-        s = tx.Search(wl.rows, fil.nchans, fil.tsamp, fil.freqs, wl.ndump,
-                      precision=args.precision, flags=tx.FLAG_CLUSTER, zapthre=ZAPTHRE)
+        s = make_search(tx.FLAG_CLUSTER)
         hpin = host.numpy()
 
         def pop_all(st, wait=True):
@@ -564,7 +560,8 @@ def run_single(args, wl):
                        "nsamples": nblk * wl.ndump, "ndump": wl.ndump, "nblocks": nblk,
                        "rows": [[sp.td, sp.dms, sp.ddm, sp.ndm] for sp in wl.rows],
                        "nsub": [i.nsub for i in infos], "dm_group": [i.dm_group for i in infos],
-                       "precision": args.precision, "parallelism": f"beam-per-gpu x{world}",
+                       "precision": args.precision, "launch_shapes": shapes,
+                       "parallelism": f"beam-per-gpu x{world}",
                        "l2": "inputs larger than L2 (raw file %.1f GB)" % (host.numel() / 1e9)},
             "clocks": clk, "e2e": e2e, "gpu_launches": stats["launches"],
             "roofline": roof, "cpu_baseline": cpu,
@@ -603,16 +600,21 @@ def lane_schedule(job, beam_ids, lanes, nsteps, bps):
 
 
 class BlockCache:
-    """Raw 8-bit blocks of the job's beams, generated once each (seeded, time-major)."""
+    """Raw 8-bit blocks of the job's beams (seeded, time-major), generated on demand and kept
+    for the later passes up to `limit` bytes."""
 
-    def __init__(self, job):
-        self.job, self.d = job, {}
+    def __init__(self, job, limit=24e9):
+        self.job, self.d, self.limit, self.bytes = job, {}, limit, 0
 
     def get(self, beam, blk):
         k = (beam, blk)
-        if k not in self.d:
-            self.d[k] = self.job.beams[beam].generate(blk * self.job.ndump, self.job.ndump)
-        return self.d[k]
+        if k in self.d:
+            return self.d[k]
+        a = self.job.beams[beam].generate(blk * self.job.ndump, self.job.ndump)
+        if self.bytes + a.nbytes <= self.limit:
+            self.d[k] = a
+            self.bytes += a.nbytes
+        return a
 
 
 class WindowInputs:
@@ -646,15 +648,18 @@ class Lanes:
     """One handle per channel count, `lanes` beams each, all searching the job's ddplan."""
 
     def __init__(self, tx, job, chans, lanes, precision, flags):
-        from transientx_gb300 import synth
         self.job, self.lanes, self.precision = job, lanes, precision
         self.s, self.infos = {}, {}
         f0 = job.beams[0]
         for C in chans:
-            s = tx.Search(job.rows, C, f0.tsamp, synth.band(C, 1712.0, 856.0), job.ndump,
-                          nbeams=lanes, precision=precision, flags=flags, zapthre=ZAPTHRE)
+            freqs = next(f.freqs for f in job.beams if f.nchans == C)
+            s = tx.Search(job.rows, C, f0.tsamp, freqs, job.ndump,
+                          nbeams=lanes, precision=precision, flags=flags | tx.FLAG_AUTOTUNE,
+                          zapthre=ZAPTHRE)
             self.s[C] = s
             self.infos[C] = [s.row_info(r) for r in range(len(job.rows))]
+            self.shapes = getattr(self, "shapes", {})
+            self.shapes[C] = [list(s.launch_shape(r)) for r in range(len(job.rows))]
 
     def push(self, item, data=None, dev=None):
         C, lane, _beam, _blk, reset = item
@@ -803,6 +808,8 @@ def run_batch(args):
     names = ["unpack", "preprocess", "stage1", "stage2", "boxcar"]
     elem = ELEM[args.precision]
 
+    shapes = {}
+
     def measure(lanes, precision, dev_inputs, flags=0, clocks=None):
         chans, steps = lane_schedule(job, mine, lanes, nsteps, bps)
         window = WindowInputs(torch, cache, steps[t_first:], "cuda" if dev_inputs else None)
@@ -810,6 +817,7 @@ def run_batch(args):
         barrier()
         ms, st = run_lanes(torch, L, cache, steps, t_first, window, dev_inputs, stream, clocks)
         infos = L.infos
+        shapes.update(L.shapes)
         L.close()
         nbytes = window.nbytes
         del window
@@ -832,7 +840,7 @@ def run_batch(args):
     nb, sm, op = [0.0] * 5, [0.0] * 5, [0.0] * 5
     f0 = job.beams[0]
     for C in chans:
-        freqs = synth.band(C, 1712.0, 856.0)
+        freqs = next(f.freqs for f in job.beams if f.nchans == C)
         for r, sp in enumerate(job.rows):
             info = infos[C][r]
             g = tst["gated"][(C, r)]
@@ -938,6 +946,9 @@ def run_batch(args):
                        "nsub": {str(C): [i.nsub for i in infos[C]] for C in chans},
                        "dm_group": {str(C): [i.dm_group for i in infos[C]] for C in chans},
                        "precision": args.precision,
+                       "launch_shapes": {str(C): shapes.get(C) for C in chans},
+                       "launch_shapes_basis": "[stage-1 shape, stage-2 variant, stage-2 KB] per "
+                                              "row, autotuned at txg_create (last pass)",
                        "parallelism": f"{args.lanes} lanes per channel count x beams sharded "
                                       f"over {world} rank(s)",
                        "l2": "inputs larger than L2 (timed raw blocks %.1f GB)" % (win_bytes / 1e9)},

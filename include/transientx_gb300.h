@@ -55,7 +55,9 @@ typedef enum {
     TXG_FLAG_DENSE = 2,        /* keep dense mxS/mxwn (Boxcar::mxS/mxwn, include/boxcar.h:40-41) */
     TXG_FLAG_KEEP_SERIES = 4,  /* keep preprocessed block and dedispersed series for inspection */
     TXG_FLAG_TIMING = 8,       /* bracket each kernel class with CUDA events (txg_get_timing) */
-    TXG_FLAG_CLUSTER = 16      /* run Cluster::run on every gated block while harvesting it */
+    TXG_FLAG_CLUSTER = 16,     /* run Cluster::run on every gated block while harvesting it */
+    TXG_FLAG_AUTOTUNE = 32     /* time the dedispersion launch shapes at txg_create and keep
+                                * the fastest per row (txg_get_launch_shape) */
 } txg_flags;
 
 /* One ddplan row: the fields of SinglePulse that SinglePulse::prepare/run read
@@ -135,6 +137,15 @@ void txg_destroy(txg_handle *h);
  * the device asynchronously and must stay unchanged until the next txg_sync. */
 int txg_push_block(txg_handle *h, int32_t beam, const uint8_t *host, int64_t nsamp);
 int txg_push_block_device(txg_handle *h, int32_t beam, const uint8_t *dev, int64_t nsamp);
+
+/* The same for a float block [nsamp][nchans] (time-major) that the caller has already
+ * unpacked and preprocessed, the DataBuffer<float> that SinglePulse::run receives
+ * (singlepulse.cpp:287, after PreprocessLite::run, dedisperse_fil.cpp:329): each row's
+ * td x fd downsample sums the floats in the 8-bit path's order, and equalize takes its mean
+ * and variance from FP64 sums in a fixed order instead of exact integer sums; the plan's
+ * channel zap (zapthre) does not apply to float blocks (PreprocessLite has done it).  The
+ * first call allocates the handle's float staging buffers; buffer rules as txg_push_block. */
+int txg_push_block_f32(txg_handle *h, int32_t beam, const float *host, int64_t nsamp);
 
 /* Start a new observation on a beam: the next block pushed to it is the first block of a new
  * file, its history, sample counter and subband rings as at txg_create.  Blocks queued
@@ -332,6 +343,18 @@ int txg_replot(const txg_replot_opts *opts, const txg_replot_cand *cands, int64_
  * number of launches of class c; classes 0 unpack, 1 preprocess+RFI, 2 stage 1,
  * 3 stage 2, 4 boxcar.  Returns the number of classes. */
 int txg_get_timing(txg_handle *h, double *ms, int64_t *launches, int32_t n);
+
+/* txg_get_timing for one ddplan row (its own accumulators, reset by this call). */
+int txg_get_row_timing(txg_handle *h, int32_t row, double *ms, int64_t *launches, int32_t n);
+
+/* The dedispersion launch shapes a row runs with: stage1 = resident stage-1 shape (time tile
+ * x coarse-DM groups per CTA), stage2 = stage-2 threads-per-CTA variant, stage2_kb = its
+ * shared-memory budget in KB (0 = default); see txg_dedisp.cu.  With TXG_FLAG_AUTOTUNE they
+ * are the fastest of a few candidates timed at txg_create (all candidates give bit-identical
+ * results; the subband count and DM group stay as planned, since they change the sums).  No
+ * reference counterpart. */
+int txg_get_launch_shape(txg_handle *h, int32_t row, int32_t *stage1, int32_t *stage2,
+                         int32_t *stage2_kb);
 
 /* The handle's CUDA stream (cudaStream_t) so callers can order or time work against it.  The
  * rows of a block run on streams of their own that fork from this one; their work joins it at

@@ -180,6 +180,8 @@ def lib() -> C.CDLL:
     L.txo_sp_destroy.argtypes = [C.c_void_p]
     L.txo_sp_run.restype = C.c_int
     L.txo_sp_run.argtypes = [C.c_void_p, u8p]
+    L.txo_sp_run_f32.restype = C.c_int
+    L.txo_sp_run_f32.argtypes = [C.c_void_p, f32p]
     L.txo_sp_nwidths.restype = C.c_int
     L.txo_sp_nwidths.argtypes = [C.c_void_p, i32p, C.c_int]
     L.txo_sp_dedisp_info.argtypes = [C.c_void_p, C.POINTER(DedispInfo)]
@@ -454,6 +456,11 @@ class SinglePulseRow:
     def run(self, raw) -> bool:
         raw = np.ascontiguousarray(raw, np.uint8)
         return bool(lib().txo_sp_run(self.h, raw))
+
+    def run_f32(self, block) -> bool:
+        """A preprocessed float block [ndump][nchan] (no channel zap)."""
+        block = np.ascontiguousarray(block, np.float32)
+        return bool(lib().txo_sp_run_f32(self.h, block))
 
     def info(self) -> DedispInfo:
         i = DedispInfo()

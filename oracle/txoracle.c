@@ -203,6 +203,26 @@ void txo_unpack_downsample(const uint8_t *raw, long n0, int nchan, int td, int f
     }
 }
 
+/* The same downsample of a float block (time-major [n0][nchan]) that the caller already
+ * preprocessed: the order of the 8-bit path (fd outer, td inner), no channel mask. */
+void txo_unpack_downsample_f32(const float *blk, long n0, int nchan, int td, int fd, float *x,
+                               long ldx)
+{
+    int nc = nchan / fd;
+    long nn = n0 / td;
+#pragma omp parallel for num_threads(nthr())
+    for (int j = 0; j < nc; j++) {
+        for (long i = 0; i < nn; i++) {
+            float acc = 0.f;
+            for (int k = 0; k < fd; k++) {
+                const long c = (long)j * fd + k;
+                for (int t = 0; t < td; t++) acc = acc + blk[(i * td + t) * (long)nchan + c];
+            }
+            x[(long)j * ldx + i] = acc;
+        }
+    }
+}
+
 /* src/singlepulse/candidate.cpp:410-418 */
 void txo_downsample_freqs(const double *f, int nchan, int fd, double *out)
 {
@@ -232,6 +252,25 @@ void txo_equalize(float *x, int nchan, long n, long ldx, uint8_t *live)
         }
         double mean = (double)s1 / (double)n;
         double var = (double)s2 / (double)n - mean * mean;
+        double sd = var > 0. ? sqrt(var) : 1.;
+        float mf = (float)mean, inv = (float)(1. / sd);
+        for (long i = 0; i < n; i++) r[i] = (r[i] - mf) * inv;
+        if (live) live[j] = var > 0. ? 1 : 0;
+    }
+}
+
+/* Equalize of a float block: the sums of the values and of their squares in the fixed FP64
+ * pattern of txo_red32 instead of exact integer sums, then the same mean, variance, standard
+ * deviation (1 when the variance is not positive) and apply as txo_equalize. */
+void txo_equalize_f32(float *x, int nchan, long n, long ldx, uint8_t *live)
+{
+    if (n <= 0) return;
+#pragma omp parallel for num_threads(nthr())
+    for (int j = 0; j < nchan; j++) {
+        float *r = x + (long)j * ldx;
+        double s1 = txo_red32(r, 0, n, 0), s2 = txo_red32(r, 0, n, 1);
+        double mean = s1 / (double)n;
+        double var = s2 / (double)n - mean * mean;
         double sd = var > 0. ? sqrt(var) : 1.;
         float mf = (float)mean, inv = (float)(1. / sd);
         for (long i = 0; i < n; i++) r[i] = (r[i] - mf) * inv;
@@ -1157,6 +1196,8 @@ void txo_sp_destroy(txo_sp *sp)
     free(sp);
 }
 
+static int sp_rest(txo_sp *sp);
+
 int txo_sp_run(txo_sp *sp, const uint8_t *raw)
 {
     const txo_row *row = &sp->row;
@@ -1164,6 +1205,24 @@ int txo_sp_run(txo_sp *sp, const uint8_t *raw)
     txo_unpack_downsample(raw, sp->ndump_raw, sp->nchan_raw, row->td, row->fd, sp->x, sp->ldx,
                           sp->mask);
     txo_equalize(sp->x, sp->nchan, sp->n, sp->ldx, sp->live);
+    return sp_rest(sp);
+}
+
+/* SinglePulse::run on a float block the caller preprocessed: no channel zap, float downsample
+ * and float equalize, then the same chain. */
+int txo_sp_run_f32(txo_sp *sp, const float *blk)
+{
+    const txo_row *row = &sp->row;
+    memset(sp->mask, 0, (size_t)sp->nchan_raw);
+    txo_unpack_downsample_f32(blk, sp->ndump_raw, sp->nchan_raw, row->td, row->fd, sp->x, sp->ldx);
+    txo_equalize_f32(sp->x, sp->nchan, sp->n, sp->ldx, sp->live);
+    return sp_rest(sp);
+}
+
+/* baseline, zaplist, rfilist, dedispersion and boxcar of one block (singlepulse.cpp:291-330) */
+static int sp_rest(txo_sp *sp)
+{
+    const txo_row *row = &sp->row;
     long nw = row->bswidth > 0.f ? (long)round((double)row->bswidth / sp->tsamp) : 0;
     txo_baseline(sp->x, sp->nchan, sp->n, sp->ldx, nw, sp->live);
     if (row->nzap > 0)

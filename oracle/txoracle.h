@@ -134,6 +134,12 @@ txo_sp *txo_sp_create(const txo_row *row, int nchan, const double *freqs, double
                       long ndump);
 void txo_sp_destroy(txo_sp *sp);
 int txo_sp_run(txo_sp *sp, const uint8_t *raw);
+/* SinglePulse::run on a preprocessed float block [ndump][nchan] (time-major): the caller's
+ * DataBuffer<float> after PreprocessLite (dedisperse_fil.cpp:329, singlepulse.cpp:287-341). */
+int txo_sp_run_f32(txo_sp *sp, const float *blk);
+void txo_unpack_downsample_f32(const float *blk, long n0, int nchan, int td, int fd, float *x,
+                               long ldx);
+void txo_equalize_f32(float *x, int nchan, long n, long ldx, uint8_t *live);
 int txo_sp_nwidths(const txo_sp *sp, int *vwn, int cap);
 void txo_sp_dedisp_info(const txo_sp *sp, txo_dedisp_info *info);
 const float *txo_sp_block(const txo_sp *sp, long *ldx, int *nchan, long *n);

@@ -78,3 +78,78 @@ def test_integration_cpp_snippet_compiles(tmp_path):
     if not shutil.which("g++"):
         pytest.skip("no g++")
     _link(tmp_path, "g++", "c++17", "block_loop.cpp", "int main() { return 0; }\n")
+
+
+def _build_fil_loop(tmp_path):
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    from transientx_gb300 import _build
+    _build.build()
+    lib = os.path.join(ROOT, "transientx_gb300")
+    exe = tmp_path / "fil_loop"
+    subprocess.run(["g++", "-std=c++17", "-O2", "-Wall", "-Werror",
+                    os.path.join(SNIPPETS, "fil_loop.cpp"), "-I", os.path.join(ROOT, "include"),
+                    "-L", lib, "-ltxgpu", f"-Wl,-rpath,{lib}", "-o", str(exe)], check=True)
+    return exe
+
+
+def test_fil_loop_compiles_against_the_class_compatible_headers(tmp_path):
+    """transientx_fil's block loop (dedisperse_fil.cpp:319-338), with the reference's class
+    names and calls -- parse(vm, search), SinglePulse::prepare/run(DataBuffer<float>&),
+    PreprocessLite, Boxcar, Cluster<double>, CandPlot -- compiles against include/compat/ and
+    links with the library."""
+    _build_fil_loop(tmp_path)
+
+
+@pytest.mark.gpu
+def test_fil_loop_finds_the_oracles_candidates(tx, oracle, tmp_path):
+    """The block loop over include/compat/ on the 256-channel configuration (ddplan
+    "1 1 0 0.5 2000 0.1 0.05", 16 subbands, 15625-sample blocks, from the block before the
+    DM-100 pulse): every searched block's candidate list equals the oracle's float chain
+    clustered by the oracle's Cluster::run rule, and the .cands file has one line each."""
+    from transientx_gb300 import synth
+    exe = _build_fil_loop(tmp_path)
+    wl = synth.WORKLOADS["nchan256_n1M_dm1000"]()
+    fil, ndump = wl.fil, wl.ndump
+    s0, nblk = 12, 4
+    raw = fil.generate(s0 * ndump, nblk * ndump)
+    (tmp_path / "obs.raw").write_bytes(raw.tobytes())
+    (tmp_path / "ddplan.txt").write_text("# td fd dms ddm ndm snrloss maxw\n"
+                                         "1 1 0 0.5 2000 0.1 0.05\n")
+    r = subprocess.run([str(exe), str(tmp_path / "obs.raw"), str(fil.nchans), repr(fil.tsamp),
+                        repr(float(fil.freqs[0])), repr(float(fil.freqs[1] - fil.freqs[0])),
+                        str(ndump), str(tmp_path / "ddplan.txt"), str(tmp_path / "obs")],
+                       capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 0, r.stdout + r.stderr
+    got = {}
+    for line in r.stdout.splitlines():
+        if line.startswith("cand "):
+            _, rid, counter, idm, isamp, wn, S = line.split()
+            got.setdefault(int(counter), []).append((int(idm), int(isamp), int(wn), float(S)))
+    nsub, group = oracle.plan_row(fil.freqs, fil.tsamp, 1, 1, 0.5, 2000, 16, 0)
+    row = oracle.make_row(td=1, fd=1, bswidth=0.1, rfi=[], dms=0.0, ddm=0.5, ndm=2000,
+                          nsub=nsub, group=group, minw=1e-4, maxw=0.05, snrloss=0.1, thre=7.0,
+                          zapthre=0.0)
+    o = oracle.SinglePulseRow(row, fil.freqs, fil.tsamp, ndump)
+    maxwn = int(o.widths().max())
+    want, ngated = {}, 0
+    for b in range(nblk):
+        blk = raw[b * ndump:(b + 1) * ndump].astype(np.float32)
+        if not o.run_f32(blk):
+            continue
+        ngated += 1
+        i = o.info()
+        pts = oracle.threshold_scan(o.mxS(), o.mxwn(), 7.0)
+        cl, _ = oracle.cluster(pts, 0.0, 0.5, i.fmax, i.fmin, i.tsamp, 1e-3, 100, 5, False, maxwn)
+        want[int(i.counter)] = [(int(c["idm"]), int(c["isamp"]), int(c["wn"]), float(c["S"]))
+                                for c in cl]
+    assert ngated == nblk - 1
+    assert sum(len(v) for v in want.values()) > 0, "the DM-100 pulse should be found"
+    for counter, cl in want.items():
+        g = got.get(counter, [])
+        assert [c[:3] for c in g] == [c[:3] for c in cl], counter
+        for a, b in zip(g, cl):
+            assert abs(a[3] - b[3]) <= 1e-4 * max(1.0, abs(b[3])), (counter, a, b)
+    cands = list(tmp_path.glob("obs_*.cands"))
+    assert len(cands) == 1
+    assert len(cands[0].read_text().splitlines()) == sum(len(v) for v in want.values())

@@ -520,3 +520,34 @@ def test_reset_beam_equals_fresh_handle(tx, prec):
                 np.testing.assert_array_equal(s.candidates(r, beam=1), fresh.candidates(r))
                 np.testing.assert_array_equal(s.cluster(r, beam=0), fresh.cluster(r))
         assert ngated >= 4
+
+
+def test_float_blocks_match_oracle(tx, oracle):
+    """txg_push_block_f32: preprocessed float blocks (non-integer values, as PreprocessLite
+    hands them to SinglePulse::run) give the oracle's float chain bit for bit: downsampled and
+    equalized block, zap windows and dedispersed series; boxcar S within 1e-4."""
+    fil, rows, ndump = small_workload()
+    orows = oracle_rows(oracle, rows, fil, ndump, tx, zapthre=0.0)
+    flags = tx.FLAG_DENSE | tx.FLAG_KEEP_SERIES
+    ngated = 0
+    with tx.Search(rows, fil.nchans, fil.tsamp, fil.freqs, ndump, flags=flags,
+                   zapthre=4.0) as s:
+        for b in range(fil.nsamples // ndump):
+            raw = fil.generate(b * ndump, ndump)
+            blk = ((raw.astype(np.float32) - np.float32(128.0)) / np.float32(12.3)
+                   + np.float32(0.37)).astype(np.float32)
+            s.push_block_f32(blk)
+            s.sync()
+            for r, o in enumerate(orows):
+                gated = o.run_f32(blk)
+                assert bool(s.row_info(r).gated) == gated
+                np.testing.assert_array_equal(s.block(r), o.block(), err_msg=f"block {b} row {r}")
+                np.testing.assert_array_equal(s.zap_ranges(0, r), o.zap_ranges(0))
+                if not gated:
+                    continue
+                ngated += 1
+                tim = s.timdata(r)
+                np.testing.assert_array_equal(tim, o.timdata(), err_msg=f"tim block {b} row {r}")
+                S, W = s.dense(r)
+                assert_boxcar_close(tim, o.widths(), S, W, o.mxS(), o.mxwn())
+    assert ngated >= 4

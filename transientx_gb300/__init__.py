@@ -29,6 +29,7 @@ ERR_TIMEOUT, ERR_STATE, ERR_NODEVICE, ERR_UNSUPPORTED = -5, -6, -7, -8
 RFI_KADANEF, RFI_ZDOT, RFI_MASK, RFI_KADANET, RFI_ZERO = 1, 2, 3, 4, 5
 PREC_FP32, PREC_BF16, PREC_FP16 = 0, 1, 2
 FLAG_AVX2_TAIL, FLAG_DENSE, FLAG_KEEP_SERIES, FLAG_TIMING, FLAG_CLUSTER = 1, 2, 4, 8, 16
+FLAG_AUTOTUNE = 32
 PRECISIONS = {"fp32": PREC_FP32, "bf16": PREC_BF16, "fp16": PREC_FP16}
 
 
@@ -106,7 +107,8 @@ EXPORTS = [
     "txg_cluster", "txg_get_timing", "txg_get_stream", "txg_strerror", "txg_version",
     "txg_describe_row", "txg_pop_result", "txg_get_mask", "txg_kadaneF_noalloc",
     "txg_get_subdata", "txg_cand_band", "txg_replot", "txg_get_timdata_q", "txg_result_ready",
-    "txg_selftest_wait", "txg_reset_beam",
+    "txg_selftest_wait", "txg_reset_beam", "txg_push_block_f32", "txg_get_launch_shape",
+    "txg_get_row_timing",
 ]
 
 _lib: Optional[C.CDLL] = None
@@ -132,6 +134,10 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.txg_push_block_device.argtypes = [vp, C.c_int32, vp, C.c_int64]
     L.txg_sync.argtypes = [vp]
     L.txg_reset_beam.argtypes = [vp, C.c_int32]
+    L.txg_push_block_f32.argtypes = [vp, C.c_int32, vp, C.c_int64]
+    L.txg_get_row_timing.argtypes = [vp, C.c_int32, vp, vp, C.c_int32]
+    L.txg_get_launch_shape.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                       C.POINTER(C.c_int32)]
     L.txg_get_row_info.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(txg_row_info)]
     L.txg_get_candidates.argtypes = [vp, C.c_int32, C.c_int32, vp, C.c_int64,
                                      C.POINTER(C.c_int64)]
@@ -397,6 +403,15 @@ class Search:
         if rc not in (OK, ERR_OVERFLOW):
             _check(rc, "txg_push_block")
 
+    def push_block_f32(self, block: np.ndarray, beam: int = 0) -> None:
+        """One preprocessed float block [ndump][nchans] (txg_push_block_f32)."""
+        blk = np.ascontiguousarray(block, np.float32)
+        if blk.shape != (self.ndump, self.nchans):
+            raise ValueError(f"block must be [{self.ndump}][{self.nchans}] float32")
+        rc = load_library().txg_push_block_f32(self.h, beam, _ptr(blk), self.ndump)
+        if rc not in (OK, ERR_OVERFLOW):
+            _check(rc, "push_block_f32")
+
     def push_block_device(self, dev_ptr: int, beam: int = 0) -> None:
         rc = load_library().txg_push_block_device(self.h, beam, int(dev_ptr), self.ndump)
         if rc not in (OK, ERR_OVERFLOW):
@@ -555,6 +570,23 @@ class Search:
         n = np.zeros(8, np.int64)
         k = load_library().txg_get_timing(self.h, _ptr(ms), _ptr(n), 8)
         return ms[:k], n[:k]
+
+    def row_timing(self, row: int) -> Tuple[np.ndarray, np.ndarray]:
+        """Per-class device time of one ddplan row since the last call (FLAG_TIMING)."""
+        ms = np.zeros(8, np.float64)
+        n = np.zeros(8, np.int64)
+        k = load_library().txg_get_row_timing(self.h, row, _ptr(ms), _ptr(n), 8)
+        if k < 0:
+            _check(k, "row_timing")
+        return ms[:k], n[:k]
+
+    def launch_shape(self, row: int = 0) -> Tuple[int, int, int]:
+        """(stage-1 shape, stage-2 variant, stage-2 KB) the row runs with
+        (txg_get_launch_shape; with FLAG_AUTOTUNE, the fastest timed at creation)."""
+        a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
+        _check(load_library().txg_get_launch_shape(self.h, row, C.byref(a), C.byref(b),
+                                                   C.byref(c)), "launch_shape")
+        return a.value, b.value, c.value
 
     def stream(self) -> int:
         s = vp()

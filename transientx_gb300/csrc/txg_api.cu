@@ -18,6 +18,7 @@
 #include <condition_variable>
 #include <cstdio>
 #include <cstdlib>
+#include <array>
 #include <cstring>
 #include <deque>
 #include <functional>
@@ -187,7 +188,6 @@ struct Workers {
 
 struct BeamRow {
     float *xh[2] = {nullptr, nullptr};
-    __half *x16 = nullptr; /* FP16 copy of the current buffer (16-bit precisions) */
     int cur = 0;
     float *ds = nullptr;
     int32_t *ranges[8] = {nullptr};
@@ -257,6 +257,14 @@ struct txg_handle {
     cudaEvent_t fork = nullptr;
     uint8_t *raw[2] = {nullptr, nullptr};
     uint8_t *stage[2] = {nullptr, nullptr}; /* pinned staging for pageable host input */
+    /* float blocks (txg_push_block_f32): device double buffer, pinned staging and their
+     * events, allocated by the first such push */
+    float *rawf[2] = {nullptr, nullptr};
+    float *stagef[2] = {nullptr, nullptr};
+    cudaEvent_t rawf_free[2] = {nullptr, nullptr};
+    cudaEvent_t rawf_loaded[2] = {nullptr, nullptr};
+    int rawf_cur = 0;
+    bool rawf_ready = false;
     cudaEvent_t raw_free[2] = {nullptr, nullptr};   /* kernels done with raw[i] */
     cudaEvent_t raw_loaded[2] = {nullptr, nullptr}; /* raw[i] copied in */
     int raw_cur = 0;
@@ -265,6 +273,8 @@ struct txg_handle {
     int prec = 0, flags = 0;
     double class_ms[NCLASS] = {0};
     long class_n[NCLASS] = {0};
+    std::vector<std::array<double, NCLASS>> row_ms; /* the same per ddplan row */
+    std::vector<std::array<long, NCLASS>> row_n;
     std::vector<void *> allocs;
 };
 
@@ -354,6 +364,11 @@ void free_all(txg_handle *h)
         if (h->stage[i]) cudaFreeHost(h->stage[i]);
         if (h->raw_free[i]) cudaEventDestroy(h->raw_free[i]);
         if (h->raw_loaded[i]) cudaEventDestroy(h->raw_loaded[i]);
+        if (h->stagef[i]) cudaFreeHost(h->stagef[i]);
+        if (h->rawf_free[i]) cudaEventDestroy(h->rawf_free[i]);
+        if (h->rawf_loaded[i]) cudaEventDestroy(h->rawf_loaded[i]);
+        h->stagef[i] = nullptr;
+        h->rawf_free[i] = h->rawf_loaded[i] = nullptr;
     }
     for (cudaStream_t s : h->rst)
         if (s) cudaStreamDestroy(s);
@@ -451,6 +466,9 @@ int harvest(txg_handle *h, BeamRow &b, Slot &sl, const RowPlan &P)
             TXG_CUDA_TRY(cudaEventElapsedTime(&ms, sl.ev[c], sl.ev[c + 1]));
             h->class_ms[c] += ms;
             h->class_n[c] += 1;
+            const size_t r = (size_t)(&P - h->rp.data());
+            h->row_ms[r][c] += ms;
+            h->row_n[r][c] += 1;
         }
     }
     b.counter = sl.counter;
@@ -521,14 +539,14 @@ int join_rows(txg_handle *h)
 }
 
 /* Queue every ddplan row of one block whose raw samples are at `raw` on the device. */
-int run_block(txg_handle *h, int beam, const uint8_t *raw)
+int run_block(txg_handle *h, int beam, const uint8_t *raw, const float *rawf = nullptr)
 {
     const long n0 = h->plan.ndump;
     const int Craw = h->plan.nchans;
     const bool timing = h->flags & TXG_FLAG_TIMING;
     int status = TXG_OK;
     const uint8_t *mask = nullptr;
-    if (h->plan.zapthre > 0.f) {
+    if (!rawf && h->plan.zapthre > 0.f) {
         BeamPrep &bp = h->prep[beam];
         launch_skzap(raw, Craw, n0, h->plan.zapthre, bp.sums, bp.stats, bp.mask, h->st);
         TXG_CUDA_TRY(cudaGetLastError());
@@ -558,14 +576,22 @@ int run_block(txg_handle *h, int beam, const uint8_t *raw)
                                            P.ldh * sizeof(float), P.H * sizeof(float), P.C,
                                            cudaMemcpyDeviceToDevice, rs));
         float *x = xcur + P.H;
-        const bool part = launch_unpack(raw, Craw, n0, P.cfg.td, P.cfg.fd, x, P.ldh, P.C, P.N, mask,
-                                        b.eqpart, rs);
+        bool part = false;
+        if (rawf)
+            launch_unpack_f32(rawf, Craw, n0, P.cfg.td, P.cfg.fd, x, P.ldh, P.C, P.N, rs);
+        else
+            part = launch_unpack(raw, Craw, n0, P.cfg.td, P.cfg.fd, x, P.ldh, P.C, P.N, mask,
+                                 b.eqpart, rs);
         TXG_CUDA_TRY(cudaEventRecord(h->row_unpacked[r], rs));
         TXG_CUDA_TRY(cudaStreamWaitEvent(h->st, h->row_unpacked[r], 0));
         if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[1], rs));
 
-        /* equalize from the unpack's integer sums; its apply rides on the baseline pass */
-        launch_eq_params(part ? b.eqpart : nullptr, x, P.ldh, P.C, P.N, b.eqp, b.live, rs);
+        /* equalize from the unpack's integer sums (float blocks: FP64 sums of the block); its
+         * apply rides on the baseline pass */
+        if (rawf)
+            launch_eq_params_f32(x, P.ldh, P.C, P.N, b.eqp, b.live, rs);
+        else
+            launch_eq_params(part ? b.eqpart : nullptr, x, P.ldh, P.C, P.N, b.eqp, b.live, rs);
         if (P.bl_nw > 0) {
             launch_colmean(x, P.ldh, P.C, P.N, b.live, b.eqp, b.z, rs);
             launch_smooth(b.z, P.N, P.bl_nw, b.b, rs);
@@ -593,15 +619,13 @@ int run_block(txg_handle *h, int beam, const uint8_t *raw)
                 launch_sub_series(x, P.ldh, P.C, P.N, b.z, b.live, rs);
             }
         }
-        /* 16-bit precisions: stage 1 reads an FP16 copy (history columns included) */
-        if (b.x16) launch_to_half(xcur, P.ldh, P.C, P.H + P.N, b.x16, rs);
         if (timing) TXG_CUDA_TRY(cudaEventRecord(sl.ev[2], rs));
 
         /* stage 1: new subband samples t in [counter-N-maxd1, counter-maxd1) */
         const long counter = b.pushed + P.N;
         const long tbase = counter - P.N - P.maxd1;
         TXG_CUDA_TRY(cudaMemsetAsync(sl.dcount, 0, 2 * sizeof(int), rs));
-        launch_stage1(xcur, b.x16, P.ldh, P.H - P.maxd1, P.C, P.N, P.nsub, P.ng, D.sub_start, D.d1,
+        launch_stage1(xcur, P.ldh, P.H - P.maxd1, P.C, P.N, P.nsub, P.ng, D.sub_start, D.d1,
                       P.maxd1, P.maxch, b.ring, P.R, pmod(tbase, P.R), h->prec, P.s1_var,
                       sl.dcount + 1, rs);
         TXG_CUDA_TRY(cudaGetLastError());
@@ -721,6 +745,78 @@ int check_beam_row(txg_handle *h, int beam, int row)
     return TXG_OK;
 }
 
+/* Timing-based choice of a row's launch shapes (TXG_FLAG_AUTOTUNE).  Every candidate adds the
+ * same values in the same order, so the results do not depend on the choice: the fastest
+ * stage-1 shape (time tile x coarse-DM groups per CTA) and stage-2 variant (threads per CTA x
+ * shared-memory window budget) are kept, each timed over three launches on the row's own
+ * buffers (beam 0) after one untimed launch.  A TXG_DEDISP_SHAPE override wins over it. */
+int autotune_row(txg_handle *h, int r)
+{
+    RowPlan &P = h->rp[r];
+    RowDev &D = h->rd[r];
+    BeamRow &b = h->br[0][r];
+    int *err = b.slot[0].dcount;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        if (e0) cudaEventDestroy(e0);
+        return fail(TXG_ERR_CUDA, "event creation failed");
+    }
+    auto time_of = [&](auto &&launch, float &ms) -> int {
+        launch();
+        TXG_CUDA_TRY(cudaEventRecord(e0, h->st));
+        for (int k = 0; k < 3; k++) launch();
+        TXG_CUDA_TRY(cudaEventRecord(e1, h->st));
+        TXG_CUDA_TRY(cudaEventSynchronize(e1));
+        TXG_CUDA_TRY(cudaGetLastError());
+        TXG_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+        return TXG_OK;
+    };
+    int rc = TXG_OK;
+    const char *env = getenv("TXG_DEDISP_SHAPE");
+    TXG_CUDA_TRY(cudaMemsetAsync(err, 0, 2 * sizeof(int), h->st));
+    if (!(env && strstr(env, "s1="))) {
+        static const int cand1[] = {0, 13, 17, 14, 16, 10, 1};
+        float best = -1.f;
+        for (int v : cand1) {
+            float ms = 0.f;
+            rc = time_of([&] {
+                launch_stage1(b.xh[0], P.ldh, P.H - P.maxd1, P.C, P.N, P.nsub, P.ng, D.sub_start,
+                              D.d1, P.maxd1, P.maxch, b.ring, P.R, 0, h->prec, v, err + 1, h->st);
+            }, ms);
+            if (rc) break;
+            if (best < 0.f || ms < best) {
+                best = ms;
+                P.s1_var = v;
+            }
+        }
+    }
+    if (!rc && !(env && (strstr(env, "s2=") || strstr(env, "s2kb=")))) {
+        static const int cand2[][2] = {{0, 0}, {1, 0}, {2, 0}, {0, 36}, {2, 36}, {1, 24}};
+        float best = -1.f;
+        for (auto &c : cand2) {
+            float ms = 0.f;
+            rc = time_of([&] {
+                launch_stage2(b.ring, P.R, P.nsub, P.G, P.cfg.ndm, P.nout, D.d2, P.s2_span, 0,
+                              h->prec, c[0], c[1], b.tim, P.nout, err + 1, h->st);
+            }, ms);
+            if (rc) break;
+            if (best < 0.f || ms < best) {
+                best = ms;
+                P.s2_var = c[0];
+                P.s2_kb = c[1];
+            }
+        }
+    }
+    int hostc[2] = {0, 0};
+    if (!rc && cudaMemcpy(hostc, err, sizeof(hostc), cudaMemcpyDeviceToHost) != cudaSuccess)
+        rc = fail(TXG_ERR_CUDA, "autotune read-back failed");
+    if (!rc && hostc[1] != 0) rc = fail(TXG_ERR_TIMEOUT, "a bounded device wait gave up while autotuning");
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (!rc) TXG_CUDA_TRY(cudaMemsetAsync(err, 0, 2 * sizeof(int), h->st));
+    return rc;
+}
+
 } // namespace
 
 extern "C" {
@@ -800,6 +896,8 @@ int txg_create(const txg_plan *plan, txg_handle **out)
     h->hcap = std::min(h->cap, HCAP_MAX);
     int rc = TXG_OK;
     h->rp.resize(plan->nrows);
+    h->row_ms.assign(plan->nrows, {});
+    h->row_n.assign(plan->nrows, {});
     for (int r = 0; r < plan->nrows && !rc; r++) {
         std::string err;
         rc = plan_row(h->rows[r], plan->nchans, h->freqs.data(), plan->tsamp, plan->ndump, h->rp[r], err);
@@ -876,7 +974,6 @@ int txg_create(const txg_plan *plan, txg_handle **out)
             BeamRow &b = h->br[beam][r];
             for (int i = 0; i < (P.N >= P.H ? 1 : 2); i++)
                 if ((rc = dalloc(h, &b.xh[i], (size_t)P.C * P.ldh))) return bail(rc);
-            if (h->prec != TXG_PREC_FP32 && (rc = dalloc(h, &b.x16, (size_t)P.C * P.ldh))) return bail(rc);
             long kmax = 1;
             for (int q = 0; q < P.cfg.nrfi; q++) {
                 const int kind = P.cfg.rfi_kind[q];
@@ -928,6 +1025,9 @@ int txg_create(const txg_plan *plan, txg_handle **out)
         }
     }
     if (cudaStreamSynchronize(h->st) != cudaSuccess) return bail(fail(TXG_ERR_CUDA, "initialisation failed"));
+    if (h->flags & TXG_FLAG_AUTOTUNE)
+        for (int r = 0; r < plan->nrows; r++)
+            if ((rc = autotune_row(h, r))) return bail(rc);
     *out = h;
     return TXG_OK;
 }
@@ -979,6 +1079,52 @@ int txg_push_block(txg_handle *h, int32_t beam, const uint8_t *host, int64_t nsa
     return rc;
 }
 
+int txg_push_block_f32(txg_handle *h, int32_t beam, const float *host, int64_t nsamp)
+{
+    DeviceScope device_scope(h);
+    if (!h || !host) return fail(TXG_ERR_ARG, "null handle or buffer");
+    if (beam < 0 || beam >= (int)h->br.size()) return fail(TXG_ERR_ARG, "beam out of range");
+    if (nsamp != h->plan.ndump) return fail(TXG_ERR_ARG, "nsamp must equal the plan's ndump");
+    const size_t count = (size_t)nsamp * h->plan.nchans;
+    if (!h->rawf_ready) { /* the first float block: its buffers (a failed attempt is retried) */
+        for (int k = 0; k < 2; k++) {
+            if (!h->rawf[k]) {
+                int rc = dalloc(h, &h->rawf[k], count);
+                if (rc) return rc;
+            }
+            if (!h->stagef[k] && cudaHostAlloc((void **)&h->stagef[k], count * sizeof(float),
+                                               cudaHostAllocDefault) != cudaSuccess) {
+                h->stagef[k] = nullptr;
+                return fail(TXG_ERR_NOMEM, "pinned staging allocation failed");
+            }
+            if ((!h->rawf_free[k] &&
+                 cudaEventCreateWithFlags(&h->rawf_free[k], cudaEventDisableTiming) != cudaSuccess) ||
+                (!h->rawf_loaded[k] &&
+                 cudaEventCreateWithFlags(&h->rawf_loaded[k], cudaEventDisableTiming) != cudaSuccess))
+                return fail(TXG_ERR_CUDA, "event creation failed");
+        }
+        h->rawf_ready = true;
+    }
+    const int i = h->rawf_cur;
+    h->rawf_cur ^= 1;
+    cudaPointerAttributes attr;
+    const bool pinned = cudaPointerGetAttributes(&attr, host) == cudaSuccess &&
+                        (attr.type == cudaMemoryTypeHost || attr.type == cudaMemoryTypeManaged);
+    const float *src = host;
+    if (!pinned) {
+        TXG_CUDA_TRY(cudaEventSynchronize(h->rawf_loaded[i]));
+        memcpy(h->stagef[i], host, count * sizeof(float));
+        src = h->stagef[i];
+    }
+    TXG_CUDA_TRY(cudaStreamWaitEvent(h->cst, h->rawf_free[i], 0));
+    TXG_CUDA_TRY(cudaMemcpyAsync(h->rawf[i], src, count * sizeof(float), cudaMemcpyHostToDevice, h->cst));
+    TXG_CUDA_TRY(cudaEventRecord(h->rawf_loaded[i], h->cst));
+    TXG_CUDA_TRY(cudaStreamWaitEvent(h->st, h->rawf_loaded[i], 0));
+    int rc = run_block(h, beam, nullptr, h->rawf[i]);
+    TXG_CUDA_TRY(cudaEventRecord(h->rawf_free[i], h->st));
+    return rc;
+}
+
 int txg_sync(txg_handle *h)
 {
     DeviceScope device_scope(h);
@@ -1016,7 +1162,6 @@ int txg_reset_beam(txg_handle *h, int32_t beam)
         const cudaStream_t rs = timing ? h->st : h->rst[r];
         for (int i = 0; i < 2; i++)
             if (b.xh[i]) TXG_CUDA_TRY(cudaMemsetAsync(b.xh[i], 0, sizeof(float) * P.C * P.ldh, rs));
-        if (b.x16) TXG_CUDA_TRY(cudaMemsetAsync(b.x16, 0, sizeof(__half) * P.C * P.ldh, rs));
         TXG_CUDA_TRY(cudaMemsetAsync(b.ring, 0, (size_t)P.ng * P.nsub * P.R * ring_elem(h->prec), rs));
         b.pushed = 0;
     }
@@ -1365,6 +1510,32 @@ int txg_describe_row(const txg_plan *plan, int32_t row, txg_row_info *info, int3
     if ((rc = finish_plan(P, row))) return rc;
     if (info) fill_info(P, info);
     copy_tables(P, d1, d2, sub_start, vwn);
+    return TXG_OK;
+}
+
+int txg_get_row_timing(txg_handle *h, int32_t row, double *ms, int64_t *launches, int32_t n)
+{
+    DeviceScope device_scope(h);
+    if (!h) return fail(TXG_ERR_ARG, "null handle");
+    if (row < 0 || row >= (int)h->rp.size()) return fail(TXG_ERR_ARG, "row out of range");
+    for (int c = 0; c < NCLASS && c < n; c++) {
+        if (ms) ms[c] = h->row_ms[row][c];
+        if (launches) launches[c] = h->row_n[row][c];
+        h->row_ms[row][c] = 0.;
+        h->row_n[row][c] = 0;
+    }
+    return NCLASS;
+}
+
+int txg_get_launch_shape(txg_handle *h, int32_t row, int32_t *stage1, int32_t *stage2,
+                         int32_t *stage2_kb)
+{
+    if (!h) return fail(TXG_ERR_ARG, "null handle");
+    if (row < 0 || row >= (int)h->rp.size()) return fail(TXG_ERR_ARG, "row out of range");
+    const RowPlan &P = h->rp[row];
+    if (stage1) *stage1 = P.s1_var;
+    if (stage2) *stage2 = P.s2_var;
+    if (stage2_kb) *stage2_kb = P.s2_kb;
     return TXG_OK;
 }
 

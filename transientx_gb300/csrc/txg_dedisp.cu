@@ -284,11 +284,14 @@ k_stage1r(const float *__restrict__ xh, long ldh, long col0, int C, long N, int 
         __syncthreads();     /* everyone's; and buffer (c+1)&1 is no longer read */
         fetch(c + 1);        /* overlaps this chunk's sums */
         const int32_t *dtab = dsm + (size_t)(c & 1) * maxch * GPC;
-        float acc[GPT][U];
+        /* the thread's samples in pairs (q, q + 1): one packed FP32 add (add.rn.f32x2, each
+         * half rounded as __fadd_rn) serves two samples of a group */
+        constexpr int UH = (U + 1) / 2;
+        float2 acc[GPT][UH];
 #pragma unroll
         for (int g = 0; g < GPT; g++)
 #pragma unroll
-            for (int q = 0; q < U; q++) acc[g][q] = 0.f;
+            for (int q = 0; q < UH; q++) acc[g][q] = make_float2(0.f, 0.f);
         for (int jj = 0; jj < jn; jj++) {
             const float *wr = win + (size_t)jj * W + al + lt;
             const int4 *dv = reinterpret_cast<const int4 *>(dtab + jj * GPC + gs * GPT);
@@ -304,15 +307,23 @@ k_stage1r(const float *__restrict__ xh, long ldh, long col0, int C, long N, int 
             /* neighbouring coarse-DM groups often share a channel's delay (it moves by a
              * third of a sample per group on average): the window values are loaded again only
              * where the delay changes (a branch uniform over the thread set) */
-            float v[U];
+            float2 v[UH];
 #pragma unroll
             for (int g = 0; g < GPT; g++) {
                 if (g == 0 || dd[g] != dd[g - 1]) {
 #pragma unroll
-                    for (int q = 0; q < U; q++) v[q] = wr[dd[g] + q * TH];
+                    for (int q = 0; q < UH; q++) {
+                        v[q].x = wr[dd[g] + 2 * q * TH];
+                        v[q].y = 2 * q + 1 < U ? wr[dd[g] + (2 * q + 1) * TH] : 0.f;
+                    }
                 }
 #pragma unroll
-                for (int q = 0; q < U; q++) acc[g][q] = __fadd_rn(acc[g][q], v[q]);
+                for (int q = 0; q < UH; q++) {
+                    if (2 * q + 1 < U)
+                        acc[g][q] = __fadd2_rn(acc[g][q], v[q]);
+                    else
+                        acc[g][q].x = __fadd_rn(acc[g][q].x, v[q].x);
+                }
             }
         }
 #pragma unroll
@@ -326,7 +337,7 @@ k_stage1r(const float *__restrict__ xh, long ldh, long col0, int C, long N, int 
                     if (u < N) {
                         long t = tbase_mod + u;
                         t = t >= R ? t - R : t;
-                        out[t] = to_store<T>(acc[g][q]);
+                        out[t] = to_store<T>((q & 1) ? acc[g][q / 2].y : acc[g][q / 2].x);
                     }
                 }
             }
@@ -353,152 +364,6 @@ __device__ __forceinline__ void addp(float &lo_acc, float &hi_acc, uint32_t v, _
 __device__ __forceinline__ void build_odd(const uint32_t *e, uint32_t *o, long nwords, int tid, int nth)
 {
     for (long k = tid; k < nwords; k += nth) o[k] = __byte_perm(e[k], e[k + 1], 0x5432);
-}
-
-/* Stage 1 on the FP16 copy of the block, two consecutive samples per 32-bit shared-memory
- * load.  Each channel window is held twice, as even-aligned pairs (the bulk copy) and as
- * odd-aligned pairs (built in shared memory), so a sample pair at any delay is one aligned
- * word.  GS thread sets share the window and take GPT coarse-DM groups each.  Sums are FP32
- * in ascending channel order; the ring stores T. */
-template <typename T, int TH, int UP, int GS, int GPT>
-__global__ void __launch_bounds__(TH * GS)
-k_stage1p(const __half *__restrict__ xh, long ldh, long col0, int C, long N, int nsub, int ng,
-          const int32_t *__restrict__ sub_start, const int32_t *__restrict__ d1, long wmax,
-          int maxch, T *__restrict__ ring, long R, long tbase_mod, int *err)
-{
-    constexpr int NT = TH * GS, TT = 2 * TH * UP, GPC = GS * GPT;
-    static_assert(GPT % 4 == 0, "delays are read four at a time");
-    extern __shared__ __align__(16) unsigned char smraw[];
-    __shared__ __align__(8) uint64_t bar;
-    __shared__ int span_sh;
-    uint32_t *words = reinterpret_cast<uint32_t *>(smraw);
-    const int s = blockIdx.y;
-    const long u0 = (long)blockIdx.x * TT;
-    const int j0 = sub_start[s], j1 = sub_start[s + 1], jn = j1 - j0;
-    const int tid = threadIdx.x, lt = tid % TH, gs = tid / TH;
-    const long cstart = (u0 + col0) & ~7L; /* 16-byte boundary */
-    const int al = (int)(u0 + col0 - cstart);
-
-    if (tid == 0) {
-        mbar_init(&bar, 1);
-        fence_mbar_init();
-        span_sh = 0;
-    }
-    __syncthreads();
-    for (int jj = tid; jj < jn; jj += NT) atomicMax(&span_sh, d1[(size_t)(ng - 1) * C + j0 + jj]);
-    __syncthreads();
-    /* halves per window: the pair at the largest delay ends inside it */
-    const long W = ((long)TT + span_sh + al + 2 + 7) / 8 * 8; /* <= wmax */
-    const long ES = (W + 8) / 2;                             /* even-pair words per channel */
-    const long OS = W / 2;                                   /* odd-pair words per channel */
-    uint32_t *ew = words, *ow = words + (size_t)jn * ES;
-    /* after the windows (sized for wmax): raw delays of the next chunk, then the word offsets
-     * of the current one */
-    int32_t *raw = reinterpret_cast<int32_t *>(words + (size_t)maxch * ((wmax + 8) / 2 + wmax / 2));
-    int32_t *dsm = raw + (size_t)maxch * GPC;
-    const int nch = (ng + GPC - 1) / GPC;
-    auto fetch = [&](int c) { /* delays of chunk c (groups past the end repeat the last one) */
-        if (c < nch) {
-            const int g0 = c * GPC, gn = min(GPC, ng - g0);
-#pragma unroll 1
-            for (int e = tid; e < jn * GPC; e += NT) {
-                const int jj = e / GPC, g = e % GPC;
-                cp_async4(&raw[e], &d1[(size_t)(g0 + (g < gn ? g : gn - 1)) * C + j0 + jj]);
-            }
-        }
-        cp_async_commit();
-    };
-    fetch(0);
-    if (tid == 0) {
-        const uint32_t bytes = (uint32_t)(W * sizeof(__half));
-        mbar_expect_tx(&bar, bytes * (uint32_t)jn);
-        for (int jj = 0; jj < jn; jj++)
-            bulk_g2s(ew + (size_t)jj * ES, xh + (long)(j0 + jj) * ldh + cstart, bytes, &bar);
-    }
-    const bool ok = mbar_wait(&bar, 0);
-    if (!__syncthreads_and(ok)) {
-        if (tid == 0) atomicExch(err, 1);
-        mbar_wait(&bar, 0);
-        cp_async_wait_all();
-        return;
-    }
-    for (int jj = 0; jj < jn; jj++) build_odd(ew + (size_t)jj * ES, ow + (size_t)jj * OS, OS, tid, NT);
-    for (int c = 0; c < nch; c++) {
-        cp_async_wait_all(); /* this thread's copies of chunk c */
-        __syncthreads();     /* everyone's; the previous chunk's offsets are no longer read */
-        /* word offset of the pair at (channel, delay): even or odd copy by the parity */
-        for (int e = tid; e < jn * GPC; e += NT) {
-            const int jj = e / GPC;
-            const int h = al + raw[e];
-            dsm[e] = (h & 1) ? (int)((size_t)jn * ES + (size_t)jj * OS + (h - 1) / 2)
-                             : (int)((size_t)jj * ES + h / 2);
-        }
-        __syncthreads();
-        fetch(c + 1); /* overlaps this chunk's sums */
-        const int g0 = c * GPC, gn = min(GPC, ng - g0);
-        float acc[GPT][2 * UP];
-#pragma unroll
-        for (int g = 0; g < GPT; g++)
-#pragma unroll
-            for (int q = 0; q < 2 * UP; q++) acc[g][q] = 0.f;
-        const uint32_t *wr = words + lt;
-        for (int jj = 0; jj < jn; jj++) {
-            const int4 *dv = reinterpret_cast<const int4 *>(dsm + jj * GPC + gs * GPT);
-            int dd[GPT];
-#pragma unroll
-            for (int gq = 0; gq < GPT / 4; gq++) {
-                const int4 d = dv[gq];
-                dd[4 * gq] = d.x;
-                dd[4 * gq + 1] = d.y;
-                dd[4 * gq + 2] = d.z;
-                dd[4 * gq + 3] = d.w;
-            }
-            /* window words loaded again only where the delay changes, as in k_stage1r */
-            uint32_t v[UP];
-#pragma unroll
-            for (int g = 0; g < GPT; g++) {
-                if (g == 0 || dd[g] != dd[g - 1]) {
-#pragma unroll
-                    for (int q = 0; q < UP; q++) v[q] = wr[dd[g] + q * TH];
-                }
-#pragma unroll
-                for (int q = 0; q < UP; q++) addp(acc[g][2 * q], acc[g][2 * q + 1], v[q], __half());
-            }
-        }
-#pragma unroll
-        for (int g = 0; g < GPT; g++) {
-            const int gc = gs * GPT + g;
-            if (gc < gn) {
-                T *out = ring + ((size_t)(g0 + gc) * nsub + s) * R;
-#pragma unroll
-                for (int q = 0; q < 2 * UP; q++) {
-                    const long u = u0 + 2 * (lt + (q >> 1) * TH) + (q & 1);
-                    if (u < N) {
-                        long t = tbase_mod + u;
-                        t = t >= R ? t - R : t;
-                        out[t] = to_store<T>(acc[g][q]);
-                    }
-                }
-            }
-        }
-    }
-}
-
-/* FP16 copy of columns [0, ncols) of the channel buffer, values clamped to the FP16 range. */
-__global__ void k_to_half(const float *__restrict__ x, long ldh, int C, long ncols4,
-                          __half *__restrict__ y)
-{
-    const long total = (long)C * ncols4;
-    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
-        const long j = i / ncols4, c4 = i - j * ncols4;
-        const float4 v = *reinterpret_cast<const float4 *>(x + j * ldh + 4 * c4);
-        const float lim = 65504.f;
-        __half2 a = __floats2half2_rn(fminf(fmaxf(v.x, -lim), lim), fminf(fmaxf(v.y, -lim), lim));
-        __half2 b = __floats2half2_rn(fminf(fmaxf(v.z, -lim), lim), fminf(fmaxf(v.w, -lim), lim));
-        __half2 *o = reinterpret_cast<__half2 *>(y + j * ldh + 4 * c4);
-        o[0] = a;
-        o[1] = b;
-    }
 }
 
 /* ---- stage 2 ---------------------------------------------------------------------------- */
@@ -789,8 +654,8 @@ constexpr size_t RESIDENT_BUDGET = 200 * 1024; /* whole-subband stage-1 windows 
 /* Largest window any stage-1 CTA needs: tile + maxd1 + alignment (delays grow with the
  * group index).  xh points at column 0 of the channel buffer; col0 = H - maxd1.  When the
  * widest subband's full window fits in shared memory the resident kernel reads every channel
- * row once; otherwise the chunked kernel (channel chunks, 16 groups per CTA) is used.  The
- * 16-bit precisions read the FP16 copy x16 with the pair kernel when its windows fit. */
+ * row once; otherwise the chunked kernel (channel chunks, 16 groups per CTA) is used.  Every
+ * precision sums the FP32 block; only the ring's element type differs. */
 template <typename T, int TH, int U, int GS, int GPT>
 static bool stage1r_try(const float *xh, long ldh, long col0, int C, long N, int nsub, int ng,
                         const int32_t *sub_start, const int32_t *d1, long maxd1, int maxch, T *ring,
@@ -804,23 +669,6 @@ static bool stage1r_try(const float *xh, long ldh, long col0, int C, long N, int
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     kern<<<dim3(nblk(N, (int)tt), nsub), TH * GS, smem, st>>>(xh, ldh, col0, C, N, nsub, ng, sub_start,
                                                               d1, wr, maxch, ring, R, tbase_mod, err);
-    return true;
-}
-
-template <typename T, int TH, int UP, int GS, int GPT>
-static bool stage1p_try(const __half *x16, long ldh, long col0, int C, long N, int nsub, int ng,
-                        const int32_t *sub_start, const int32_t *d1, long maxd1, int maxch, T *ring,
-                        long R, long tbase_mod, int *err, cudaStream_t st)
-{
-    const long tt = 2L * TH * UP;
-    const long w = (tt + maxd1 + 7 + 2 + 7) / 8 * 8;
-    const size_t smem =
-        (size_t)maxch * ((w + 8) / 2 + w / 2) * 4 + 2 * (size_t)maxch * GS * GPT * sizeof(int32_t);
-    if (smem > RESIDENT_BUDGET) return false;
-    auto kern = k_stage1p<T, TH, UP, GS, GPT>;
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    kern<<<dim3(nblk(N, (int)tt), nsub), TH * GS, smem, st>>>(x16, ldh, col0, C, N, nsub, ng, sub_start,
-                                                              d1, w, maxch, ring, R, tbase_mod, err);
     return true;
 }
 
@@ -841,25 +689,23 @@ static void stage1_chunked(const float *xh, long ldh, long col0, int C, long N, 
                                                 wmax, ring, R, tbase_mod, err);
 }
 
-/* Resident launch shapes (threads per set x samples per thread, thread sets x groups each):
- *   FP32 windows: 0 = 32x16 16x4 (default), 1 = 256x2 1x16, 2 = 512x1 1x16, 3 = 256x2 2x8,
- *                 4 = 256x2 2x16, 5 = 256x1 2x8, 6 = 256x2 4x4, 7 = 128x4 4x8, 8 = 256x4 2x8,
- *                 9 = 128x4 2x8, 10 = 128x4 8x4, 11 = 64x8 8x4, 12 = 64x8 4x4, 13 = 64x8 16x4,
- *                 14 = 64x8 8x8, 15 = 64x16 8x4, 16 = 256x2 4x8, 17 = 32x8 16x8
- *   16-bit pairs: 0 = 32x8 16x4 (default), 1 = 256x1 1x16, 2 = 256x1 2x8, 3 = 256x1 2x16,
- *                 4 = 256x1 4x4, 5 = 128x1 4x8, 6 = 256x1 4x8, 7 = 64x4 8x4, 8 = 128x2 8x4,
- *                 9 = 64x4 16x4, 10 = 128x2 4x8, 11 = 64x8 8x4
+/* Resident launch shapes (threads per set x samples per thread, thread sets x groups each),
+ * the same for every ring precision:
+ *   0 = 32x16 16x4 (default), 1 = 256x2 1x16, 2 = 512x1 1x16, 3 = 256x2 2x8, 4 = 256x2 2x16,
+ *   5 = 256x1 2x8, 6 = 256x2 4x4, 7 = 128x4 4x8, 8 = 256x4 2x8, 9 = 128x4 2x8, 10 = 128x4 8x4,
+ *   11 = 64x8 8x4, 12 = 64x8 4x4, 13 = 64x8 16x4, 14 = 64x8 8x8, 15 = 64x16 8x4,
+ *   16 = 256x2 4x8, 17 = 32x8 16x8
  * Every channel step loads the thread's delays (broadcast 16-byte loads, two shared-memory
  * wavefronts each) and then one window element per sample for each distinct delay among its
  * groups: many samples per thread and one warp per set keep the delay loads a small share of
  * the shared-memory traffic (measured on the 4096-channel workload: 32x16 16x4 took stage 1
  * from 185 to 159 ms per 20 blocks against 256x2 4x8; loading only where the delay changes,
- * 159 to 114 ms FP32 and 111 to 102 ms for the 16-bit pairs).  A shape whose windows do not fit falls back to 256x2 1x16, then
- * to the chunked kernel (any negative variant selects the chunked kernel directly).  The
- * 16-bit fallbacks past the pair kernels read the FP32 block (one rounding fewer than the FP16
- * copy), so their series can differ in the last bits from the pair kernels'. */
+ * 159 to 114 ms; a sweep of all shapes on the GB300 kept 32x16 16x4, the 1024-thread 64x8
+ * 16x4 at 60 registers being 3 % slower).  A shape whose windows do not fit falls back to
+ * 256x2 1x16, then to the chunked kernel (any negative variant selects the chunked kernel
+ * directly). */
 template <typename T>
-static void stage1_dispatch(const float *xh, const __half *x16, long ldh, long col0, int C, long N,
+static void stage1_dispatch(const float *xh, long ldh, long col0, int C, long N,
                             int nsub, int ng, const int32_t *sub_start, const int32_t *d1, long maxd1,
                             int maxch, T *ring, long R, long tbase_mod, int var, int *err,
                             cudaStream_t st)
@@ -870,75 +716,46 @@ static void stage1_dispatch(const float *xh, const __half *x16, long ldh, long c
     }
     bool done = false;
 #define TXG_ARGS xh, ldh, col0, C, N, nsub, ng, sub_start, d1, maxd1, maxch, ring, R, tbase_mod, err, st
-#define TXG_PARGS x16, ldh, col0, C, N, nsub, ng, sub_start, d1, maxd1, maxch, ring, R, tbase_mod, err, st
-    if constexpr (!std::is_same<T, float>::value) {
-        if (x16) {
-            switch (var) {
-            case 1: break;
-            case 2: done = stage1p_try<T, 256, 1, 2, 8>(TXG_PARGS); break;
-            case 3: done = stage1p_try<T, 256, 1, 2, 16>(TXG_PARGS); break;
-            case 4: done = stage1p_try<T, 256, 1, 4, 4>(TXG_PARGS); break;
-            case 5: done = stage1p_try<T, 128, 1, 4, 8>(TXG_PARGS); break;
-            case 6: done = stage1p_try<T, 256, 1, 4, 8>(TXG_PARGS); break;
-            case 7: done = stage1p_try<T, 64, 4, 8, 4>(TXG_PARGS); break;
-            case 8: done = stage1p_try<T, 128, 2, 8, 4>(TXG_PARGS); break;
-            case 9: done = stage1p_try<T, 64, 4, 16, 4>(TXG_PARGS); break;
-            case 10: done = stage1p_try<T, 128, 2, 4, 8>(TXG_PARGS); break;
-            case 11: done = stage1p_try<T, 64, 8, 8, 4>(TXG_PARGS); break;
-            default: done = stage1p_try<T, 32, 8, 16, 4>(TXG_PARGS); break;
-            }
-            if (!done) done = stage1p_try<T, 256, 1, 1, 16>(TXG_PARGS);
-        }
-    } else {
-        switch (var) {
-        case 1: break;
-        case 2: done = stage1r_try<T, 512, 1, 1, 16>(TXG_ARGS); break;
-        case 3: done = stage1r_try<T, 256, 2, 2, 8>(TXG_ARGS); break;
-        case 4: done = stage1r_try<T, 256, 2, 2, 16>(TXG_ARGS); break;
-        case 5: done = stage1r_try<T, 256, 1, 2, 8>(TXG_ARGS); break;
-        case 6: done = stage1r_try<T, 256, 2, 4, 4>(TXG_ARGS); break;
-        case 7: done = stage1r_try<T, 128, 4, 4, 8>(TXG_ARGS); break;
-        case 8: done = stage1r_try<T, 256, 4, 2, 8>(TXG_ARGS); break;
-        case 9: done = stage1r_try<T, 128, 4, 2, 8>(TXG_ARGS); break;
-        case 10: done = stage1r_try<T, 128, 4, 8, 4>(TXG_ARGS); break;
-        case 11: done = stage1r_try<T, 64, 8, 8, 4>(TXG_ARGS); break;
-        case 12: done = stage1r_try<T, 64, 8, 4, 4>(TXG_ARGS); break;
-        case 13: done = stage1r_try<T, 64, 8, 16, 4>(TXG_ARGS); break;
-        case 14: done = stage1r_try<T, 64, 8, 8, 8>(TXG_ARGS); break;
-        case 15: done = stage1r_try<T, 64, 16, 8, 4>(TXG_ARGS); break;
-        case 16: done = stage1r_try<T, 256, 2, 4, 8>(TXG_ARGS); break;
-        case 17: done = stage1r_try<T, 32, 8, 16, 8>(TXG_ARGS); break;
-        default: done = stage1r_try<T, 32, 16, 16, 4>(TXG_ARGS); break;
-        }
+    switch (var) {
+    case 1: break;
+    case 2: done = stage1r_try<T, 512, 1, 1, 16>(TXG_ARGS); break;
+    case 3: done = stage1r_try<T, 256, 2, 2, 8>(TXG_ARGS); break;
+    case 4: done = stage1r_try<T, 256, 2, 2, 16>(TXG_ARGS); break;
+    case 5: done = stage1r_try<T, 256, 1, 2, 8>(TXG_ARGS); break;
+    case 6: done = stage1r_try<T, 256, 2, 4, 4>(TXG_ARGS); break;
+    case 7: done = stage1r_try<T, 128, 4, 4, 8>(TXG_ARGS); break;
+    case 8: done = stage1r_try<T, 256, 4, 2, 8>(TXG_ARGS); break;
+    case 9: done = stage1r_try<T, 128, 4, 2, 8>(TXG_ARGS); break;
+    case 10: done = stage1r_try<T, 128, 4, 8, 4>(TXG_ARGS); break;
+    case 11: done = stage1r_try<T, 64, 8, 8, 4>(TXG_ARGS); break;
+    case 12: done = stage1r_try<T, 64, 8, 4, 4>(TXG_ARGS); break;
+    case 13: done = stage1r_try<T, 64, 8, 16, 4>(TXG_ARGS); break;
+    case 14: done = stage1r_try<T, 64, 8, 8, 8>(TXG_ARGS); break;
+    case 15: done = stage1r_try<T, 64, 16, 8, 4>(TXG_ARGS); break;
+    case 16: done = stage1r_try<T, 256, 2, 4, 8>(TXG_ARGS); break;
+    case 17: done = stage1r_try<T, 32, 8, 16, 8>(TXG_ARGS); break;
+    default: done = stage1r_try<T, 32, 16, 16, 4>(TXG_ARGS); break;
     }
     if (!done) done = stage1r_try<T, 256, 2, 1, 16>(TXG_ARGS);
 #undef TXG_ARGS
-#undef TXG_PARGS
     if (!done) stage1_chunked<T>(xh, ldh, col0, C, N, nsub, ng, sub_start, d1, maxd1, maxch, ring, R, tbase_mod, err, st);
 }
 
-void launch_stage1(const float *xh, const __half *x16, long ldh, long col0, int C, long N, int nsub,
+void launch_stage1(const float *xh, long ldh, long col0, int C, long N, int nsub,
                    int ng, const int32_t *sub_start, const int32_t *d1, long maxd1, int maxch, void *ring,
                    long R, long tbase_mod, int prec, int var, int *err, cudaStream_t st)
 {
     if (prec == TXG_PREC_BF16)
-        stage1_dispatch<__nv_bfloat16>(xh, x16, ldh, col0, C, N, nsub, ng, sub_start, d1, maxd1, maxch,
+        stage1_dispatch<__nv_bfloat16>(xh, ldh, col0, C, N, nsub, ng, sub_start, d1, maxd1, maxch,
                                        (__nv_bfloat16 *)ring, R, tbase_mod, var, err, st);
     else if (prec == TXG_PREC_FP16)
-        stage1_dispatch<__half>(xh, x16, ldh, col0, C, N, nsub, ng, sub_start, d1, maxd1, maxch,
+        stage1_dispatch<__half>(xh, ldh, col0, C, N, nsub, ng, sub_start, d1, maxd1, maxch,
                                 (__half *)ring, R, tbase_mod, var, err, st);
     else
-        stage1_dispatch<float>(xh, nullptr, ldh, col0, C, N, nsub, ng, sub_start, d1, maxd1, maxch,
+        stage1_dispatch<float>(xh, ldh, col0, C, N, nsub, ng, sub_start, d1, maxd1, maxch,
                                (float *)ring, R, tbase_mod, var, err, st);
 }
 
-void launch_to_half(const float *x, long ldh, int C, long ncols, __half *y, cudaStream_t st)
-{
-    const long n4 = (ncols + 3) / 4;
-    const long total = (long)C * n4;
-    const long blocks = std::min<long>((total + 255) / 256, 152L * 8);
-    k_to_half<<<(unsigned)blocks, 256, 0, st>>>(x, ldh, C, n4, y);
-}
 
 /* DMs per stage-2 CTA for a group of G fine DMs (one chunk per group when G <= 32). */
 static int stage2_kpc(int G) { return G <= 8 ? 8 : G <= 16 ? 16 : G <= 24 ? 24 : 32; }

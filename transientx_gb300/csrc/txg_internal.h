@@ -79,6 +79,12 @@ bool launch_unpack(const uint8_t *raw, int C_raw, long n0, int td, int fd, float
 /* equalize: per-channel (mean, 1/sd) and live flags; the apply is fused into the next pass */
 void launch_eq_params(const unsigned long long *part, const float *x, long ldx, int C, long N,
                       float2 *eqp, uint8_t *live, cudaStream_t st);
+/* Float blocks: transpose + sum-downsample of a time-major float block, and equalize's
+ * (mean, 1/sd) pairs and live flags from FP64 sums in the fixed red32 pattern. */
+void launch_unpack_f32(const float *blk, int C_raw, long n0, int td, int fd, float *x, long ldx,
+                       int C, long N, cudaStream_t st);
+void launch_eq_params_f32(const float *x, long ldx, int C, long N, float2 *eqp, uint8_t *live,
+                          cudaStream_t st);
 /* x <- standardised x, minus b on live channels when b is given */
 void launch_eq_apply(float *x, long ldx, int C, long N, const float2 *eqp, const float *b,
                      const uint8_t *live, cudaStream_t st);
@@ -105,13 +111,11 @@ void launch_mask(float *x, long ldx, int C, long N, int tdk, int fdk, float thr,
 /* zp: C (mean, 1/sd) pairs of scratch */
 void launch_zdot(float *x, long ldx, int C, long N, float *s, double *sstats, float2 *zp,
                  cudaStream_t st);
-/* x16: FP16 copy of the channel buffer (same layout, used by the 16-bit precisions, may be
- * null); var: resident launch shape (0 = default; see txg_dedisp.cu). */
-void launch_stage1(const float *xh, const __half *x16, long ldh, long col0, int C, long N, int nsub,
+/* Every precision reads the FP32 channel buffer and accumulates in FP32; the ring stores
+ * FP32, BF16 or FP16 (prec).  var: resident launch shape (0 = default; see txg_dedisp.cu). */
+void launch_stage1(const float *xh, long ldh, long col0, int C, long N, int nsub,
                    int ng, const int32_t *sub_start, const int32_t *d1, long maxd1, int maxch,
                    void *ring, long R, long tbase_mod, int prec, int var, int *err, cudaStream_t st);
-/* FP16 copy (values clamped to +-65504) of columns [0, ncols) of a [C][ldh] buffer */
-void launch_to_half(const float *x, long ldh, int C, long ncols, __half *y, cudaStream_t st);
 long stage2_span(const int32_t *d2h, int nsub, int G, long ndm);
 long stage2_window(long span);
 /* s2_var: FP32 threads per CTA (0 = 32, 1 = 64, 2 = 128); s2_kb: shared-memory budget of

@@ -455,6 +455,67 @@ __global__ void k_unpack_direct(const uint8_t *__restrict__ raw, int C_raw, int 
     x[(long)j * ldx + i] = acc;
 }
 
+/* ---- float blocks (a caller's DataBuffer<float> after its own preprocessing) ----------- */
+/* Transpose + td x fd sum-downsample of a time-major float block [n0][C_raw] into the
+ * channel-major buffer: x[j][i] = sum over k < fd (outer) and t < td (inner) of
+ * blk[(i*td + t)*C_raw + j*fd + k], added in that order from 0.0f (the order of the 8-bit
+ * path and of candidate.cpp:395-407).  A CTA computes FT_J x FT_I outputs: its threads read
+ * the raw rows along channels (coalesced), sum in registers, and a shared-memory transpose
+ * writes along time. */
+constexpr int FT_J = 32, FT_I = 32;
+
+__global__ void __launch_bounds__(FT_J * 8) k_unpack_f32(const float *__restrict__ blk, int C_raw,
+                                                        int td, int fd, float *__restrict__ x,
+                                                        long ldx, int C, long N)
+{
+    __shared__ float tile[FT_J][FT_I + 1];
+    const int jj = threadIdx.x, iy = threadIdx.y; /* 32 channels x 8 sample rows */
+    const int j = blockIdx.y * FT_J + jj;
+    const long i0 = (long)blockIdx.x * FT_I;
+#pragma unroll
+    for (int r = 0; r < FT_I / 8; r++) {
+        const int ii = r * 8 + iy;
+        const long i = i0 + ii;
+        float acc = 0.f;
+        if (j < C && i < N) {
+            for (int k = 0; k < fd; k++) {
+                const float *src = blk + (i * td) * (long)C_raw + (long)j * fd + k;
+                for (int t = 0; t < td; t++) acc = __fadd_rn(acc, src[(long)t * C_raw]);
+            }
+        }
+        tile[jj][ii] = acc;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < FT_J / 8; r++) {
+        const int cj = r * 8 + iy;
+        const long i = i0 + jj;
+        if (blockIdx.y * FT_J + cj < C && i < N)
+            x[(long)(blockIdx.y * FT_J + cj) * ldx + i] = tile[cj][jj];
+    }
+}
+
+/* Equalize statistics of a float block (one warp per channel): the sums of the values and of
+ * their squares in the fixed FP64 reduction pattern of red32x2, then the same mean, variance,
+ * (mean, 1/sd) pair and live flag as the 8-bit path's exact integer sums give. */
+__global__ void __launch_bounds__(256) k_eq_params_f32(const float *__restrict__ x, long ldx, int C,
+                                                       long N, float2 *__restrict__ eqp,
+                                                       uint8_t *__restrict__ live)
+{
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= C) return;
+    double s1, s2;
+    red32x2<1>(x + (long)w * ldx, nullptr, N, lane, s1, s2);
+    if (lane == 0) {
+        const double dn = (double)N;
+        double mean = __ddiv_rn(s1, dn);
+        double var = __dsub_rn(__ddiv_rn(s2, dn), __dmul_rn(mean, mean));
+        double sd = var > 0. ? __dsqrt_rn(var) : 1.;
+        eqp[w] = make_float2(__double2float_rn(mean), __double2float_rn(__ddiv_rn(1., sd)));
+        if (live) live[w] = var > 0. ? 1 : 0;
+    }
+}
+
 /* ---- equalize: exact integer statistics of the integer-valued downsampled block ---------- */
 /* Per channel (one warp): the exact sums of the values and of their squares -- from the
  * unpack's per-tile partial sums when `part` is given, else from the block -- give
@@ -1030,6 +1091,20 @@ void launch_eq_params(const unsigned long long *part, const float *x, long ldx, 
                       float2 *eqp, uint8_t *live, cudaStream_t st)
 {
     k_eq_params<<<nblk((long)C * 32, 256), 256, 0, st>>>(part, eq_part_tiles(N), x, ldx, C, N, eqp, live);
+}
+
+void launch_unpack_f32(const float *blk, int C_raw, long n0, int td, int fd, float *x, long ldx,
+                       int C, long N, cudaStream_t st)
+{
+    (void)n0;
+    dim3 grid(nblk(N, FT_I), nblk(C, FT_J));
+    k_unpack_f32<<<grid, dim3(FT_J, 8), 0, st>>>(blk, C_raw, td, fd, x, ldx, C, N);
+}
+
+void launch_eq_params_f32(const float *x, long ldx, int C, long N, float2 *eqp, uint8_t *live,
+                          cudaStream_t st)
+{
+    k_eq_params_f32<<<nblk((long)C * 32, 256), 256, 0, st>>>(x, ldx, C, N, eqp, live);
 }
 
 void launch_eq_apply(float *x, long ldx, int C, long N, const float2 *eqp, const float *b,

@@ -215,6 +215,16 @@ def beams64(seed: int = 4, nbeams: int = 64) -> BeamJob:
     return BeamJob("beams64_nchan1024_4096", beams, rows, seglen_ndump(tsamp, [1, 2, 4]))
 
 
+def beams16_nchan8192(seed: int = 5, nbeams: int = 16, nsamples: int = 1 << 23) -> BeamJob:
+    """16 beams of an 8192-channel search-mode observation at 16 us (1200-1800 MHz), 2^23
+    samples each: the single-beam 8192-channel workload's RFI (5% sinusoid channels, zero-DM
+    impulses at 1/s) and bursts (32 us-5 ms, DM 10-5000, S/N 8-30), beam b seeded seed + b;
+    the five-row ddplan to DM 5000 with td 1/2/4/8/16 and maxw 0.01 s."""
+    beams = [nchan8192_dm5000(seed=seed + b, nsamples=nsamples).fil for b in range(nbeams)]
+    wl = nchan8192_dm5000(seed=seed, nsamples=1 << 16)
+    return BeamJob("beams16_nchan8192_dm5000", beams, wl.rows, wl.ndump)
+
+
 def replot_candidates(n: int, nchan: int = 4096, seed: int = 9, dm: float = 500.0,
                       width: float = 2e-3, tbin: float = 76e-6, nwidth: int = 20):
     """Candidates as replot_fil cuts them (replot_fil.cpp:300-306): nbin = (delay across the
@@ -240,4 +250,4 @@ def replot_candidates(n: int, nchan: int = 4096, seed: int = 9, dm: float = 500.
 WORKLOADS = {"nchan256_n1M_dm1000": nchan256_single, "nchan4096_n2M_rfi_dm3000": nchan4096_rfi,
              "nchan8192_n8M_dm5000": nchan8192_dm5000}
 # workloads of many beams (BeamJob)
-JOBS = {"beams64_nchan1024_4096": beams64}
+JOBS = {"beams64_nchan1024_4096": beams64, "beams16_nchan8192_dm5000": beams16_nchan8192}
