@@ -764,7 +764,9 @@ def class_times(tx, job, chans, lanes, precision, cache, steps, t_first, ntimed)
     L.sync()
     L.drain(junk, wait=True)
     for s in L.s.values():
-        s.timing()  # reset the accumulators
+        s.timing()  # reset the accumulators, the handle's and each row's
+        for r in range(len(job.rows)):
+            s.row_timing(r)
     stats = new_stats()
     for st in steps[t_first:t_first + ntimed]:
         for C in chans:
@@ -775,8 +777,9 @@ def class_times(tx, job, chans, lanes, precision, cache, steps, t_first, ntimed)
             L.s[C].sync(allow_overflow=True)
         L.drain(stats, wait=True)
     cls = {C: L.s[C].timing() for C in chans}
+    rows = {C: [L.s[C].row_timing(r) for r in range(len(job.rows))] for C in chans}
     L.close()
-    return cls, stats
+    return cls, rows, stats
 
 
 def run_batch(args):
@@ -833,8 +836,8 @@ def run_batch(args):
     value = work / (ms / 1e3)
 
     # per-class times and the roofline of the dominant class
-    cls, tst = class_times(tx, job, chans, args.lanes, args.precision, cache, steps, t_first,
-                           min(K, 2))
+    cls, cls_rows, tst = class_times(tx, job, chans, args.lanes, args.precision, cache, steps,
+                                     t_first, min(K, 2))
     cls_ms = [sum(float(cls[C][0][c]) for C in chans) for c in range(5)]
     cls_n = [sum(int(cls[C][1][c]) for C in chans) for c in range(5)]
     nb, sm, op = [0.0] * 5, [0.0] * 5, [0.0] * 5
@@ -876,6 +879,38 @@ def run_batch(args):
                         "frac": sm_ach / sm_peak,
                         "peak_basis": f"{NSM} SMs x {SMEM_BYTES_PER_CLK} B/clock x median SM clock"}
     roof["alu"] = alu_roofline(op, cls_ms, sm_clk)
+    # per ddplan row (stage): its serialised class times, DM-trial rate and rooflines
+    per_row = []
+    for r, sp in enumerate(job.rows):
+        rms = [sum(float(cls_rows[C][r][0][c]) for C in chans) for c in range(5)]
+        work_r, nbr, balg_r = 0.0, [0.0] * 5, 0.0
+        for C in chans:
+            info = infos[C][r]
+            g = tst["gated"][(C, r)]
+            work_r += g * info.ndm * info.nsamples
+            cb = class_bytes(info, sp, C, job.ndump, tst["ncand"][(C, r)] / max(1, g), elem)
+            for c in range(5):
+                nbr[c] += cb[c] * (tst["blocks"][C] if c < 3 else g)
+            balg_r += tst["blocks"][C] * 2.0 * info.nsub * info.ngroup * info.ndump * elem
+        tot = sum(rms)
+        topr = int(np.argmax(rms))
+        gbps = [nbr[c] / (rms[c] / 1e3) / 1e9 if rms[c] > 0 else None for c in range(5)]
+        per_row.append({
+            "row": r, "td": sp.td, "dms": sp.dms, "ddm": sp.ddm, "ndm": sp.ndm,
+            "class_ms": {names[c]: rms[c] for c in range(5)},
+            "dm_trial_samples_per_s": work_r / (tot / 1e3) if tot > 0 else None,
+            "dominant": names[topr],
+            "dominant_hbm_frac": gbps[topr] / peak if gbps[topr] else None,
+            "class_algorithmic_GBps": {names[c]: gbps[c] for c in range(5)},
+            "subband_series_frac": balg_r / (tot / 1e3) / 1e9 / peak if tot > 0 else None})
+    row_sum = [sum(pr["class_ms"][names[c]] for pr in per_row) for c in range(5)]
+    roof["per_row_sums_match"] = all(abs(row_sum[c] - cls_ms[c]) <= 1e-3 * max(1.0, cls_ms[c])
+                                     for c in range(5))
+    roof["per_row"] = per_row
+    roof["per_row_basis"] = ("the class-timing pass's CUDA-event times per ddplan row (rows "
+                             "serialised); dominant_hbm_frac = that class's algorithmic bytes / "
+                             "its time / peak; subband_series_frac = the row's stage-1 series "
+                             "written and read once / the row's time / peak")
     balg = 0.0
     for C in chans:
         rows_info = infos[C]
