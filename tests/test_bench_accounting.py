@@ -122,13 +122,13 @@ def test_alu_roofline_of_the_bench_workload():
 
 
 def test_profiled_stage1_traffic_matches_the_algorithmic_bytes():
-    """The DRAM traffic per stage-1 launch that bench.py reports (one ncu capture, mean over the
+    """The DRAM traffic per stage-1 launch that bench.py reports (an ncu capture scaled to the
     three rows' launches) is the algorithmic stage-1 bytes of those launches within 10 %:
     each channel window crosses DRAM once and each subband sample is written once."""
     import transientx_gb300 as tx
     from transientx_gb300 import synth
     wl = synth.WORKLOADS["nchan4096_n2M_rfi_dm3000"](nsamples=1 << 16)
-    for prec, elem in (("fp32", 4),):
+    for prec, elem in (("fp32", 4), ("fp16", 2)):
         alg = []
         for r, sp in enumerate(wl.rows):
             info = tx.describe_row(wl.rows, r, wl.fil.nchans, wl.fil.tsamp, wl.fil.freqs,
