@@ -10,8 +10,9 @@ from test_gpu_pipeline import oracle_rows, small_workload
 
 pytestmark = pytest.mark.gpu
 
-FP32_SHAPES = ["s1=16", "s1=1", "s1=11", "s1=14", "s1=-1", "s2=1", "s2=2,s2kb=36", "s2=0,s2kb=8"]
-PAIR_SHAPES = ["s1=16", "s1=1", "s1=11", "s1=-1", "s2=1", "s2=2,s2kb=36"]
+FP32_SHAPES = ["s1=16", "s1=1", "s1=11", "s1=14", "s1=-1", "s2=1", "s2=2,s2kb=36", "s2=0,s2kb=8",
+               "s2=3", "s2=5"]
+PAIR_SHAPES = ["s1=16", "s1=1", "s1=11", "s1=-1", "s2=1", "s2=2,s2kb=36", "s2=3", "s2=4"]
 
 
 def _series(tx, rows, fil, ndump, prec="fp32"):
@@ -72,7 +73,8 @@ def test_autotuned_shapes_give_the_same_series(tx, prec, monkeypatch):
         for r in range(len(rows)):
             s1, s2, kb = s.launch_shape(r)
             assert s1 in (0, 13, 17, 14, 16, 10, 1)
-            assert (s2, kb) in ((0, 0), (1, 0), (2, 0), (0, 36), (2, 36), (1, 24))
+            assert (s2, kb) in ((0, 0), (1, 0), (2, 0), (0, 36), (2, 36), (1, 24), (3, 0),
+                                (4, 0), (5, 0))
         for b in range(fil.nsamples // ndump):
             s.push_block(fil.generate(b * ndump, ndump))
             s.sync()

@@ -791,7 +791,8 @@ int autotune_row(txg_handle *h, int r)
         }
     }
     if (!rc && !(env && (strstr(env, "s2=") || strstr(env, "s2kb=")))) {
-        static const int cand2[][2] = {{0, 0}, {1, 0}, {2, 0}, {0, 36}, {2, 36}, {1, 24}};
+        static const int cand2[][2] = {{0, 0}, {1, 0}, {2, 0}, {0, 36}, {2, 36}, {1, 24},
+                                       {3, 0}, {4, 0}, {5, 0}};
         float best = -1.f;
         for (auto &c : cand2) {
             float ms = 0.f;

@@ -941,12 +941,18 @@ static void stage2_dispatch(int var, const void *ring, long R, int nsub, int G, 
                             const int32_t *d2, long span, long t0_mod, float *tim, long ldt,
                             size_t budget, int *err, cudaStream_t st)
 {
+    /* variants 3-5: the thread shapes of 0-2 with half the DMs of a group per CTA (8 for
+     * groups up to 24, 16 for 32): half the accumulators, so more CTAs per SM, each subband
+     * window loaded by twice as many CTAs; every DM's sum is the same */
+    const int kfull = stage2_kpc(G);
+    const int kuse = var >= 3 ? (kfull == 32 ? 16 : 8) : kfull;
+    const int v = var >= 3 ? var - 3 : var;
 #define TXG_S2(K)                                                                                   \
     if constexpr (PAIRS)                                                                            \
-        stage2p_var<T, K>(var, ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, budget, err, st); \
+        stage2p_var<T, K>(v, ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, budget, err, st); \
     else                                                                                            \
-        stage2_var<T, K>(var, ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, budget, err, st)
-    switch (stage2_kpc(G)) {
+        stage2_var<T, K>(v, ring, R, nsub, G, ndm, nout, d2, span, t0_mod, tim, ldt, budget, err, st)
+    switch (kuse) {
     case 8: TXG_S2(8); break;
     case 16: TXG_S2(16); break;
     case 24: TXG_S2(24); break;

@@ -118,8 +118,9 @@ void launch_stage1(const float *xh, long ldh, long col0, int C, long N, int nsub
                    void *ring, long R, long tbase_mod, int prec, int var, int *err, cudaStream_t st);
 long stage2_span(const int32_t *d2h, int nsub, int G, long ndm);
 long stage2_window(long span);
-/* s2_var: FP32 threads per CTA (0 = 32, 1 = 64, 2 = 128); s2_kb: shared-memory budget of
- * one stage-2 CTA in KB, 0 = the kernel's default (CTAs per SM follow from it) */
+/* s2_var: threads per CTA (0 = 32, 1 = 64, 2 = 128; 3-5 the same with half a group's DMs per
+ * CTA); s2_kb: shared-memory budget of one stage-2 CTA in KB, 0 = the kernel's default (CTAs
+ * per SM follow from it) */
 void launch_stage2(const void *ring, long R, int nsub, int G, long ndm, long nout,
                    const int32_t *d2, long span, long t0_mod, int prec, int s2_var, int s2_kb,
                    float *tim, long ldt, int *err, cudaStream_t st);
