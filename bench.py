@@ -59,6 +59,8 @@ def parse_args():
     ap.add_argument("--preroll", type=int, default=16, help="blocks per lane before warm-up")
     ap.add_argument("--replot", type=int, default=0,
                     help="time the replot chain on this many 4096-channel candidates instead")
+    ap.add_argument("--replot-pageable", action="store_true",
+                    help="replot: pageable host buffers instead of page-locked ones")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp32", action="store_true", help="skip the FP32 same-job passes")
@@ -999,6 +1001,15 @@ def run_replot(args):
     import transientx_gb300 as tx
     from transientx_gb300 import synth
     cands = synth.replot_candidates(args.replot)
+    if not args.replot_pageable:
+        # page-locked host buffers: the cut data crosses to the device at full copy bandwidth
+        import torch
+        keep = []
+        for c in cands:
+            t = torch.empty(c["data"].shape, dtype=torch.float32, pin_memory=True)
+            t.numpy()[:] = c["data"]
+            keep.append(t)
+            c["data"] = t.numpy()
     for _ in range(args.warmup):
         tx.replot(cands)
     ts = []
@@ -1011,6 +1022,7 @@ def run_replot(args):
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3,
             "higher_is_better": True, "data": "synthetic",
             "config": {"workload": "replot_nchan4096", "candidates": args.replot,
+                       "host_buffers": "pageable" if args.replot_pageable else "pinned",
                        "shape": list(cands[0]["data"].shape), "tbin": cands[0]["tbin"],
                        "dm": cands[0]["dm"], "width": cands[0]["width"]},
             "ms_per_candidate": per * 1e3 / args.replot,
