@@ -25,14 +25,29 @@ CASES = {  # name: (workload, row)
     "nchan4096_row0": ("nchan4096_n2M_rfi_dm3000", 0),
     "nchan4096_row1": ("nchan4096_n2M_rfi_dm3000", 1),
     "nchan4096_row2": ("nchan4096_n2M_rfi_dm3000", 2),
+    # a 1024-channel beam of the 64-beam job (64 subbands, DM groups of 8/8/7)
+    "beams64_nchan1024_row0": ("beams64:1024", 0),
+    "beams64_nchan1024_row2": ("beams64:1024", 2),
+    # 8192 channels at 16 us: 62 496-sample rows (the segmented boxcar) and the td-16 row
+    "nchan8192_row0": ("nchan8192_n8M_dm5000", 0),
+    "nchan8192_row4": ("nchan8192_n8M_dm5000", 4),
 }
 ZAPTHRE = 4.0  # the bench's PreprocessLite channel-zap threshold
 NGATED = 2
 
 
 def _workload(name):
+    """A single-beam workload, or "beams64:<C>": the 64-beam job's first beam of C channels
+    that carries a pulse in every row's DM range, as a single-beam workload."""
     from transientx_gb300 import synth
-    return synth.WORKLOADS[name]()
+    if not name.startswith("beams64:"):
+        return synth.WORKLOADS[name]()
+    C = int(name.split(":")[1])
+    job = synth.beams64()
+    ranges = [(sp.dms, sp.dms + sp.ndm * sp.ddm) for sp in job.rows]
+    fil = next(f for f in job.beams if f.nchans == C and
+               all(any(lo <= p[1] < hi for p in f.pulses) for lo, hi in ranges))
+    return synth.Workload(name, fil, job.rows, job.ndump)
 
 
 def plan_blocks(tx, wl, r):
