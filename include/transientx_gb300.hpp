@@ -6,7 +6,8 @@
  *   txgpu::parse_ddplan - ddplan rows "td fd dms ddm ndm snrloss maxw [rfi opts]"
  *                         (singlepulse.cpp:407-456)
  *   txgpu::Search       - prepare (SinglePulse::prepare, singlepulse.cpp:206-254) for all rows,
- *                         run(block) (the block-loop body, dedisperse_fil.cpp:324-337)
+ *                         run(block) (the block-loop body, dedisperse_fil.cpp:324-337) on 8-bit
+ *                         or preprocessed float blocks, reset(beam) between observations
  *   txgpu::Search::cluster - Cluster<double>::run's candlist (cluster.cpp:63-161) as
  *                         (idm, isamp, wn, S) tuples, the order CandPlot::plot consumes
  *   txgpu::Boxcar       - the public members of Boxcar (include/boxcar.h:31-43) for one row
@@ -284,6 +285,17 @@ public:
     void run_device(const uint8_t *dev_block, int beam = 0)
     {
         push(txg_push_block_device(h_, beam, dev_block, ndump_));
+    }
+    /* one preprocessed float block [ndump][nchans] (txg_push_block_f32) */
+    void run_f32(const float *block, int beam = 0) { push(txg_push_block_f32(h_, beam, block, ndump_)); }
+    /* the next block pushed to `beam` starts a new observation (txg_reset_beam) */
+    void reset(int beam = 0) { check(txg_reset_beam(h_, beam), "txg_reset_beam"); }
+    /* {stage-1 shape, stage-2 variant, stage-2 KB} of a row (txg_get_launch_shape) */
+    std::tuple<int, int, int> launch_shape(int row) const
+    {
+        int32_t a = 0, b = 0, c = 0;
+        check(txg_get_launch_shape(h_, row, &a, &b, &c), "txg_get_launch_shape");
+        return std::make_tuple(a, b, c);
     }
     void sync() { push(txg_sync(h_)); }
 

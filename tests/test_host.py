@@ -236,3 +236,17 @@ def test_oracle_planner_equals_host_planner(tx, oracle):
             info = tx.describe_row(rows, r, C, tsamp, f, ndump)[0]
             assert oracle.plan_row(f, tsamp, sp.td, sp.fd, sp.ddm, sp.ndm, sp.nsub,
                                    sp.dm_group) == (info.nsub, info.dm_group), (C, r)
+
+
+def test_new_entry_points_refuse_bad_handles_and_rows(tx):
+    """txg_reset_beam, txg_push_block_f32, txg_get_launch_shape and txg_get_row_timing refuse a
+    null handle with TXG_ERR_ARG before touching any device (a host without a GPU runs this)."""
+    import ctypes
+    L = tx.load_library()
+    i32 = ctypes.c_int32()
+    buf = np.zeros(16, np.float32)
+    assert L.txg_reset_beam(None, 0) == tx.ERR_ARG
+    assert L.txg_push_block_f32(None, 0, buf.ctypes.data, 1) == tx.ERR_ARG
+    assert L.txg_get_launch_shape(None, 0, ctypes.byref(i32), ctypes.byref(i32),
+                                  ctypes.byref(i32)) == tx.ERR_ARG
+    assert L.txg_get_row_timing(None, 0, None, None, 0) == tx.ERR_ARG
