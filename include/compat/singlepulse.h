@@ -288,14 +288,16 @@ private:
     std::shared_ptr<txg_handle> gpu_;
 };
 
-/* rfi option words of a ddplan line or of the rfi option (singlepulse.cpp:350-372,432-451) */
-inline void txg_compat_rfi_words(const std::vector<std::string> &w, size_t i, SinglePulse &sp)
+/* rfi option words of a ddplan line or of the rfi option (singlepulse.cpp:350-372,432-451);
+ * an rfilist entry of the JSON configuration takes no zap (singlepulse.cpp:525-540) */
+inline void txg_compat_rfi_words(const std::vector<std::string> &w, size_t i, SinglePulse &sp,
+                                 bool zap = true)
 {
     for (; i < w.size(); i++) {
         if ((w[i] == "mask" || w[i] == "kadaneF" || w[i] == "kadaneT") && i + 2 < w.size()) {
             sp.rfilist.push_back({w[i], w[i + 1], w[i + 2]});
             i += 2;
-        } else if (w[i] == "zap" && i + 2 < w.size()) {
+        } else if (zap && w[i] == "zap" && i + 2 < w.size()) {
             sp.zaplist.emplace_back(std::stod(w[i + 1]), std::stod(w[i + 2]));
             i += 2;
         } else if (w[i] == "zero" || w[i] == "zdot") {
@@ -305,7 +307,9 @@ inline void txg_compat_rfi_words(const std::vector<std::string> &w, size_t i, Si
 }
 
 /* parse(vm, search) of singlepulse.cpp:343-459: the command-line options into one row, or
- * with --ddplan one row per ddplan line ("td fd dms ddm ndm snrloss maxw [rfi words]") */
+ * with --ddplan one row per ddplan line ("td fd dms ddm ndm snrloss maxw [rfi words]").  As in
+ * the reference one SinglePulse is carried down the lines, so a line's zap and rfi words stay
+ * in the zaplist and rfilist of every later row. */
 template <class VariablesMap>
 void parse(VariablesMap &vm, std::vector<SinglePulse> &search)
 {
@@ -341,6 +345,7 @@ void parse(VariablesMap &vm, std::vector<SinglePulse> &search)
     sp.savetim = vm.count("savetim");
     sp.format = vm["format"].template as<std::string>();
     if (!vm.count("ddplan")) {
+        sp.id = 1;
         search.push_back(sp);
         return;
     }
@@ -359,22 +364,22 @@ void parse(VariablesMap &vm, std::vector<SinglePulse> &search)
         std::vector<std::string> p;
         for (std::string w; ls >> w;) p.push_back(w);
         if (p.size() < 7) continue;
-        SinglePulse r = sp;
-        r.td = std::stoi(p[0]);
-        r.fd = std::stoi(p[1]);
-        r.dms = std::stod(p[2]);
-        r.ddm = std::stod(p[3]);
-        r.ndm = std::stol(p[4]);
-        r.snrloss = std::stof(p[5]);
-        r.maxw = std::stof(p[6]);
-        txg_compat_rfi_words(p, 7, r);
-        r.id = ++id;
-        search.push_back(r);
+        sp.td = std::stoi(p[0]);
+        sp.fd = std::stoi(p[1]);
+        sp.dms = std::stod(p[2]);
+        sp.ddm = std::stod(p[3]);
+        sp.ndm = std::stol(p[4]);
+        sp.snrloss = std::stof(p[5]);
+        sp.maxw = std::stof(p[6]);
+        txg_compat_rfi_words(p, 7, sp);
+        sp.id = ++id;
+        search.push_back(sp);
     }
 }
 
 /* parse_json(vm, config, search) of singlepulse.cpp:461-545: one row per entry of
- * config["ddplan"] */
+ * config["ddplan"]; as in the reference one SinglePulse is carried down the entries, so an
+ * entry's zaplist and rfilist stay in every later row's */
 template <class VariablesMap, class Json>
 void parse_json(VariablesMap &vm, Json &config, std::vector<SinglePulse> &search)
 {
@@ -388,43 +393,42 @@ void parse_json(VariablesMap &vm, Json &config, std::vector<SinglePulse> &search
     int id = 0;
     auto rows = config["ddplan"];
     for (auto c = rows.begin(); c != rows.end(); ++c) {
-        SinglePulse r = sp;
         auto ds = (*c)["downsample"], bl = (*c)["baseline"], rf = (*c)["rfi"];
         auto dd = (*c)["subdedispersion"], bx = (*c)["boxcar"], cl = (*c)["clustering"];
-        r.td = ds["td"];
-        r.fd = ds["fd"];
-        r.bswidth = bl["width"];
-        r.dms = dd["dms"];
-        r.ddm = dd["ddm"];
-        r.ndm = dd["ndm"];
-        r.overlap = dd["overlap"];
-        r.bandlimit = rf["bandlimit"];
-        r.bandlimitKT = rf["bandlimitKT"];
-        r.widthlimit = rf["widthlimit"];
-        r.threMask = rf["threMask"];
-        r.threKadaneF = rf["threKadaneF"];
-        r.threKadaneT = rf["threKadaneT"];
-        r.minw = bx["minw"];
-        r.snrloss = bx["snrloss"];
-        r.maxw = bx["maxw"];
-        r.iqr = bx["iqr"];
-        r.thre = cl["thre"];
-        r.radius_smearing = (double)(cl["radius"]) / 1000.;
-        r.kvalue = cl["neighbors"];
-        r.maxncand = cl["maxncand"];
-        r.minpts = cl["minpts"];
-        r.remove_cand_with_maxwidth = cl["drop"];
+        sp.td = ds["td"];
+        sp.fd = ds["fd"];
+        sp.bswidth = bl["width"];
+        sp.dms = dd["dms"];
+        sp.ddm = dd["ddm"];
+        sp.ndm = dd["ndm"];
+        sp.overlap = dd["overlap"];
+        sp.bandlimit = rf["bandlimit"];
+        sp.bandlimitKT = rf["bandlimitKT"];
+        sp.widthlimit = rf["widthlimit"];
+        sp.threMask = rf["threMask"];
+        sp.threKadaneF = rf["threKadaneF"];
+        sp.threKadaneT = rf["threKadaneT"];
+        sp.minw = bx["minw"];
+        sp.snrloss = bx["snrloss"];
+        sp.maxw = bx["maxw"];
+        sp.iqr = bx["iqr"];
+        sp.thre = cl["thre"];
+        sp.radius_smearing = (double)(cl["radius"]) / 1000.;
+        sp.kvalue = cl["neighbors"];
+        sp.maxncand = cl["maxncand"];
+        sp.minpts = cl["minpts"];
+        sp.remove_cand_with_maxwidth = cl["drop"];
         auto zl = rf["zaplist"];
         for (auto z = zl.begin(); z != zl.end(); ++z)
-            r.zaplist.emplace_back((double)z->front(), (double)z->back());
+            sp.zaplist.emplace_back((double)z->front(), (double)z->back());
         auto rl = rf["rfilist"];
         for (auto e = rl.begin(); e != rl.end(); ++e) {
             std::vector<std::string> w;
             for (auto item = e->begin(); item != e->end(); ++item) w.push_back(*item);
-            txg_compat_rfi_words(w, 0, r);
+            txg_compat_rfi_words(w, 0, sp, false);
         }
-        r.id = ++id;
-        search.push_back(r);
+        sp.id = ++id;
+        search.push_back(sp);
     }
 }
 

@@ -153,3 +153,46 @@ def test_fil_loop_finds_the_oracles_candidates(tx, oracle, tmp_path):
     cands = list(tmp_path.glob("obs_*.cands"))
     assert len(cands) == 1
     assert len(cands[0].read_text().splitlines()) == sum(len(v) for v in want.values())
+
+
+def test_parse_and_parse_json_rows(tmp_path):
+    """parse(vm, search) and parse_json(vm, config, search) of include/compat/singlepulse.h,
+    instantiated over stand-ins for the options map and the JSON type
+    (tests/snippets/parse_config.cpp): the fields of every row follow singlepulse.cpp:343-545
+    -- radius in ms becomes seconds, a ddplan line's seven numbers override the options, the
+    command-line rfi words come first, and one SinglePulse is carried down the ddplan lines
+    and JSON entries, so a row keeps every earlier row's zap and rfi entries.  An rfilist entry
+    of the JSON configuration takes no zap.  No GPU call is made."""
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    from transientx_gb300 import _build
+    _build.build()
+    lib = os.path.join(ROOT, "transientx_gb300")
+    exe = tmp_path / "parse_config"
+    subprocess.run(["g++", "-std=c++17", "-Wall", "-Werror", "-Wno-unused-variable",
+                    os.path.join(SNIPPETS, "parse_config.cpp"), "-I", os.path.join(ROOT, "include"),
+                    "-L", lib, "-ltxgpu", f"-Wl,-rpath,{lib}", "-o", str(exe)], check=True)
+    (tmp_path / "ddplan.txt").write_text(
+        "# td fd dms ddm ndm snrloss maxw\n"
+        "1 1 0 0.1 5000 0.1 0.05 zap 1300 1310 kadaneT 3 5\n"
+        "  2 1 500 0.2 5000 0.1 0.05 mask 4 8 zero\n"
+        "\n"
+        "not a row\n")
+    json_rows = [
+        "row 1 td 2 fd 1 dms 500 ddm 0.2 ndm 5000 snrloss 0.1 maxw 0.05 bswidth 0.2 thre 6.5 "
+        "radius 0.002 minpts 3 iqr 1 nzap 1 rfi kadaneF 8 4 zdot",
+        "row 2 td 4 fd 1 dms 1500 ddm 0.2 ndm 5000 snrloss 0.1 maxw 0.05 bswidth 0.2 thre 6.5 "
+        "radius 0.002 minpts 3 iqr 1 nzap 2 rfi kadaneF 8 4 zdot zero"]
+    out = subprocess.run([str(exe), str(tmp_path / "ddplan.txt")], capture_output=True,
+                         text=True, check=True).stdout.splitlines()
+    assert out == [
+        "row 1 td 1 fd 1 dms 0 ddm 0.1 ndm 5000 snrloss 0.1 maxw 0.05 bswidth 0.1 thre 7 "
+        "radius 0.001 minpts 5 iqr 0 nzap 2 rfi zdot kadaneF 8 4 kadaneT 3 5",
+        "row 2 td 2 fd 1 dms 500 ddm 0.2 ndm 5000 snrloss 0.1 maxw 0.05 bswidth 0.1 thre 7 "
+        "radius 0.001 minpts 5 iqr 0 nzap 2 rfi zdot kadaneF 8 4 kadaneT 3 5 mask 4 8 zero",
+    ] + json_rows
+    # without a ddplan the options make one row, id 1
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines()
+    assert out == [
+        "row 1 td 1 fd 1 dms 0 ddm 1 ndm 1000 snrloss 0.1 maxw 0.02 bswidth 0.1 thre 7 "
+        "radius 0.001 minpts 5 iqr 0 nzap 1 rfi zdot kadaneF 8 4"] + json_rows
