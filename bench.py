@@ -707,6 +707,30 @@ class Lanes:
         self.s = {}
 
 
+def h2d_rates(torch, window):
+    """Host-to-device rate of each block of the page-locked window, timed with CUDA events
+    just before the timed pass that pushes them (outside it).  On the GB300 machines the rate
+    of page-locked memory differs between allocations and over time (3-20 GB/s for some
+    blocks, about 210 GB/s for others, whatever the device is doing), which bounds the e2e
+    rate of jobs whose blocks are large."""
+    hv = window.host.numpy()
+    ends = list(window.offsets[1:]) + [window.nbytes]
+    sizes = [int(e) - int(o) for o, e in zip(window.offsets, ends)]
+    scratch = torch.empty(max(sizes), dtype=torch.uint8, device="cuda")
+    evs = []
+    for o, n in zip(window.offsets, sizes):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        scratch[:n].copy_(torch.from_numpy(hv[int(o):int(o) + n]), non_blocking=True)
+        e1.record()
+        evs.append((n, e0, e1))
+    torch.cuda.synchronize()
+    r = sorted(n / (a.elapsed_time(b) / 1e3) / 1e9 for n, a, b in evs)
+    del scratch
+    return {"blocks": len(r), "min_GBps": round(r[0], 1), "median_GBps": round(r[len(r) // 2], 1),
+            "max_GBps": round(r[-1], 1)}
+
+
 def new_stats():
     return {"work": 0, "launches": 0, "overflow": 0, "d2h": 0, "clusters": 0, "pushed": 0,
             "blocks": collections.Counter(), "ncand": collections.Counter(),
@@ -726,6 +750,8 @@ def run_lanes(torch, L, cache, steps, t_first, window, dev_inputs, stream, clock
     L.sync()
     L.drain(junk, wait=True)
     stats = new_stats()
+    if not dev_inputs:
+        stats["h2d_window"] = h2d_rates(torch, window)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     window.k = 0
@@ -949,6 +975,7 @@ def run_batch(args):
                "h2d_bytes_per_step": win_bytes // K,
                "d2h_bytes_per_step": st_e["d2h"] // K,
                "clusters_per_step": st_e["clusters"] / K, "overflow_blocks": st_e["overflow"],
+               "h2d_window": st_e["h2d_window"],
                "includes": "H2D from pinned host memory, candidate read-back and Cluster::run "
                            "of every block inside the library, every block's results popped "
                            "(as they become ready, the rest after the final sync); host wall "
