@@ -13,10 +13,10 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-# the TransientX source tree whose boxcar.cpp, cluster.cpp and candidate.cpp are compiled in
-# place (read-only); TXREF_TREE overrides the checkout's usual mount point.  Where no tree
-# exists (a machine without the reference) only the oracle itself is built.
-REF_TREE = os.environ.get("TXREF_TREE", "/root/reference")
+# The TransientX source tree whose boxcar.cpp, cluster.cpp and candidate.cpp are compiled in
+# place (read-only) comes from the caller of build() or from TXREF_TREE; without one (a machine
+# without the reference) only the oracle itself is built and the tests that need the
+# reference's own code skip.
 
 f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
@@ -31,11 +31,16 @@ RFI_KADANET = 4
 RFI_ZERO = 5
 
 
-def build(ref: bool = True) -> None:
-    """Compile the oracle; also the reference harness when the reference tree is present."""
+def build(ref: bool = True, tree: str | None = None) -> None:
+    """Compile the oracle; with `ref`, also the reference harness from the TransientX source
+    tree `tree` (default: the TXREF_TREE environment variable) when one is given."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    if ref and os.path.isdir(REF_TREE):
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_TREE}"], check=True)
+    tree = tree or os.environ.get("TXREF_TREE")
+    if ref and tree:
+        if not os.path.isdir(os.path.join(tree, "src", "singlepulse")):
+            raise FileNotFoundError(f"TXREF_TREE={tree!r} is not a TransientX source tree "
+                                    "(no src/singlepulse)")
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={tree}"], check=True)
 
 
 class Cand(C.Structure):

@@ -15,7 +15,8 @@ def pytest_configure(config):
 @pytest.fixture(scope="session")
 def oracle():
     import pyoracle
-    pyoracle.build(ref=True)
+    from __graft_entry__ import reference_tree
+    pyoracle.build(ref=True, tree=reference_tree())
     return pyoracle
 
 

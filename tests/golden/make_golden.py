@@ -2,7 +2,8 @@
 and Cluster<double> (src/singlepulse/cluster.cpp), compiled in place from the reference tree
 by oracle/Makefile (`make -C oracle ref`), on seeded inputs.
 
-Run from the repository root where the reference tree exists:
+Run from the repository root where the reference tree exists (TXREF_TREE names it when it is
+not at its usual mount point):
     python tests/golden/make_golden.py
 Writes tests/golden/boxcar.npz and tests/golden/cluster.npz.
 """
@@ -12,8 +13,10 @@ import sys
 import numpy as np
 
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import pyoracle as O  # noqa: E402
+from __graft_entry__ import reference_tree  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
 
@@ -34,8 +37,8 @@ def boxcar_inputs(seed=11, ndm=8, n=1500):
 
 
 def main():
-    O.build(ref=True)
-    assert O.ref_available("scalar"), "reference harness not built (is the reference tree present?)"
+    O.build(ref=True, tree=reference_tree())
+    assert O.ref_available("scalar"), "reference harness not built (set TXREF_TREE to the reference tree)"
     tim, vwn = boxcar_inputs()
     out = {"tim": tim, "vwn": vwn}
     variants = ["scalar"] + (["avx2"] if O.ref_available("avx2") else [])
