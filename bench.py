@@ -716,7 +716,10 @@ def h2d_rates(torch, window):
     hv = window.host.numpy()
     ends = list(window.offsets[1:]) + [window.nbytes]
     sizes = [int(e) - int(o) for o, e in zip(window.offsets, ends)]
-    scratch = torch.empty(max(sizes), dtype=torch.uint8, device="cuda")
+    try:
+        scratch = torch.empty(max(sizes), dtype=torch.uint8, device="cuda")
+    except torch.cuda.OutOfMemoryError:
+        return {"unmeasured": "no device memory for a block-sized scratch beside the lanes"}
     evs = []
     for o, n in zip(window.offsets, sizes):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -727,6 +730,7 @@ def h2d_rates(torch, window):
     torch.cuda.synchronize()
     r = sorted(n / (a.elapsed_time(b) / 1e3) / 1e9 for n, a, b in evs)
     del scratch
+    torch.cuda.empty_cache()
     return {"blocks": len(r), "min_GBps": round(r[0], 1), "median_GBps": round(r[len(r) // 2], 1),
             "max_GBps": round(r[-1], 1)}
 
